@@ -1,0 +1,82 @@
+/*
+ * pyrsgm_gb300.h -- additions of pyrsgm-gb300 that have no counterpart in
+ * the reference API: debug access to the internal volumes, a C surface over
+ * pyrsgm::StereoMatcher, and sizing helpers.  Declarations here sit beside
+ * the drop-in pyrsgm_c.h / pyrsgm.h, never instead of them.
+ */
+#ifndef PYRSGM_GB300_H
+#define PYRSGM_GB300_H
+
+#include <stddef.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Workspace debug flags. */
+#define PYRSGM_GB300_DEBUG_AGGREGATED 1  /* keep the final aggregated cost volume in the workspace */
+
+int pyrsgm_gb300_workspace_set_debug(void* workspace, int flags);
+
+/* Device pointers to the workspace's matching-cost volume and aggregation
+ * volume ([y][x][d] int16, d innermost, numDisparities labels) after the last
+ * call on it.  The aggregation volume holds the final summed path costs only
+ * when PYRSGM_GB300_DEBUG_AGGREGATED was set before that call. */
+int pyrsgm_gb300_workspace_volumes(void* workspace, const short** cost, const short** aggregated,
+                                   int* width, int* height, int* numDisparities);
+
+/* Copy both volumes (width*height*numDisparities int16 each) into caller
+ * device buffers (either may be NULL), asynchronously on `stream`. */
+int pyrsgm_gb300_workspace_copy_volumes(void* workspace, short* cost, short* aggregated, cudaStream_t stream);
+
+/* Device bytes one workspace of this geometry allocates. */
+size_t pyrsgm_gb300_workspace_bytes(int width, int height, int numDisparities);
+
+/* The adaptive-P2 table: d_table[i] (256 ints, device) = the effective P2 for
+ * |I(p) - I(p-r)| = i, after the reference's parameter sanitising. */
+int pyrsgm_gb300_p2_table(int* d_table, int P2, float p2Alpha, float p2Beta, float p2LowerMult, float p2UpperMult,
+                          cudaStream_t stream);
+
+/* pyrsgm::Params as a C struct (same fields, same defaults). */
+typedef struct pyrsgm_gb300_params {
+    int num_disparities, min_disparity, block_size, cost_mode;
+    int p1, p2, uniqueness_ratio, disp12_max_diff;
+    int lr_check, median_filter, num_paths, pre_filter_cap;
+    int pyramid_levels, pyramid_coarse_disparities, pyramid_max_disparity;
+    float pyramid_min_confidence;
+    int adaptive_p2;
+    float p2_alpha, p2_beta, p2_lower_mult, p2_upper_mult;
+} pyrsgm_gb300_params;
+
+void pyrsgm_gb300_default_params(pyrsgm_gb300_params* p);
+/* pyrsgm::validateParams; returns 0, or -1 with the exception text in err. */
+int pyrsgm_gb300_validate_params(const pyrsgm_gb300_params* in, pyrsgm_gb300_params* out, char* err,
+                                 size_t err_len);
+
+/* pyrsgm::StereoMatcher through C.  create returns NULL (message in err) on
+ * failure; compute returns 0 or -1 (message in err). */
+void* pyrsgm_gb300_matcher_create(int width, int height, const pyrsgm_gb300_params* p, char* err,
+                                  size_t err_len);
+void pyrsgm_gb300_matcher_destroy(void* matcher);
+int pyrsgm_gb300_matcher_compute(void* matcher, const unsigned char* d_left, size_t left_pitch,
+                                 const unsigned char* d_right, size_t right_pitch, short* d_disp16,
+                                 size_t disp16_pitch, float* d_disp32, size_t disp32_pitch, float* d_conf,
+                                 size_t conf_pitch, cudaStream_t stream, char* err, size_t err_len);
+/* Level geometry of StereoMatcher(width, height, p) without allocating:
+ * writes 7 ints per level (as pyrsgm_gb300_matcher_level_info) into out35
+ * and returns the number of levels, or -1 (message in err). */
+int pyrsgm_gb300_level_geometry(int width, int height, const pyrsgm_gb300_params* p, int* out35, char* err,
+                                size_t err_len);
+/* out[7] = level, width, height, num_labels, max_disparity, block_size, refine */
+int pyrsgm_gb300_matcher_level_info(void* matcher, int level, int* out7);
+int pyrsgm_gb300_matcher_num_levels(void* matcher);
+size_t pyrsgm_gb300_matcher_device_bytes(void* matcher);
+
+const char* pyrsgm_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYRSGM_GB300_H */

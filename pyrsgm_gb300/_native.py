@@ -1,0 +1,91 @@
+"""ctypes bindings of libpyrsgm_gb300.so (the C ABI in include/pyrsgm/).
+
+The library is built in-tree by pyrsgm_gb300.build; importing this module
+never falls back to anything else: a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpyrsgm_gb300.so")
+
+_vp, _u8p, _i16p, _f32p = C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p
+_sz, _i, _f = C.c_size_t, C.c_int, C.c_float
+
+
+class Params(C.Structure):
+    """pyrsgm_gb300_params: pyrsgm::Params as a C struct."""
+    _fields_ = [(n, _i) for n in (
+        "num_disparities", "min_disparity", "block_size", "cost_mode",
+        "p1", "p2", "uniqueness_ratio", "disp12_max_diff",
+        "lr_check", "median_filter", "num_paths", "pre_filter_cap",
+        "pyramid_levels", "pyramid_coarse_disparities", "pyramid_max_disparity")] + [
+        ("pyramid_min_confidence", _f), ("adaptive_p2", _i),
+        ("p2_alpha", _f), ("p2_beta", _f), ("p2_lower_mult", _f), ("p2_upper_mult", _f)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "pyrsgm_create_workspace": (_vp, []),
+    "pyrsgm_destroy_workspace": (None, [_vp]),
+    "pyrsgm_workspace_reserve": (_i, [_vp, _i, _i, _i]),
+    "pyrsgm_compute_single_scale": (_i, [_vp, _u8p, _u8p, _i16p, _f32p, _f32p, _sz, _sz, _sz, _sz, _sz,
+                                         _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i,
+                                         _f, _f, _f, _f, _vp]),
+    "pyrsgm_compute_level": (_i, [_vp, _u8p, _u8p, _i16p, _f32p, _i16p, _f32p, _f32p,
+                                  _sz, _sz, _sz, _sz, _sz, _sz, _sz,
+                                  _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i,
+                                  _f, _i, _f, _f, _f, _f, _vp]),
+    "pyrsgm_pyrdown_u8": (_i, [_u8p, _sz, _i, _i, _u8p, _sz, _i, _i, _vp]),
+    "pyrsgm_gb300_workspace_set_debug": (_i, [_vp, _i]),
+    "pyrsgm_gb300_workspace_volumes": (_i, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_i),
+                                            C.POINTER(_i), C.POINTER(_i)]),
+    "pyrsgm_gb300_workspace_copy_volumes": (_i, [_vp, _i16p, _i16p, _vp]),
+    "pyrsgm_gb300_workspace_bytes": (_sz, [_i, _i, _i]),
+    "pyrsgm_gb300_p2_table": (_i, [_vp, _i, _f, _f, _f, _f, _vp]),
+    "pyrsgm_gb300_default_params": (None, [C.POINTER(Params)]),
+    "pyrsgm_gb300_validate_params": (_i, [C.POINTER(Params), C.POINTER(Params), C.c_char_p, _sz]),
+    "pyrsgm_gb300_matcher_create": (_vp, [_i, _i, C.POINTER(Params), C.c_char_p, _sz]),
+    "pyrsgm_gb300_matcher_destroy": (None, [_vp]),
+    "pyrsgm_gb300_matcher_compute": (_i, [_vp, _u8p, _sz, _u8p, _sz, _i16p, _sz, _f32p, _sz, _f32p, _sz,
+                                          _vp, C.c_char_p, _sz]),
+    "pyrsgm_gb300_matcher_level_info": (_i, [_vp, _i, C.POINTER(_i)]),
+    "pyrsgm_gb300_matcher_num_levels": (_i, [_vp]),
+    "pyrsgm_gb300_level_geometry": (_i, [_i, _i, C.POINTER(Params), C.POINTER(_i), C.c_char_p, _sz]),
+    "pyrsgm_gb300_matcher_device_bytes": (_sz, [_vp]),
+    "pyrsgm_gb300_version": (C.c_char_p, []),
+}
+
+# Entry points declared in include/pyrsgm/*.h (checked by the tests).
+EXPORTS = tuple(_SIGS)
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load the native library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"pyrsgm-gb300 native library missing at {LIB_PATH}; "
+                               "build it with pyrsgm_gb300.build.build()")
+        h = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = h
+    return _lib
+
+
+def optional_symbol(name: str, restype, argtypes):
+    """Bind an entry point that not every build declares in _SIGS."""
+    fn = getattr(lib(), name)
+    fn.restype = restype
+    fn.argtypes = argtypes
+    return fn

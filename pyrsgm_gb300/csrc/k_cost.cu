@@ -1,0 +1,406 @@
+// k_cost.cu -- per-pixel stages of one level: pyrDown, census / BT features,
+// refine-label preparation, the adaptive-P2 table and the matching-cost
+// volume.  Integer arithmetic, clamps and sentinels follow the reference
+// kernels cited at each function (reference file:line).
+#include "sgm_common.cuh"
+#include "sgm_launch.h"
+
+namespace pg {
+
+// ---------------------------------------------------------------------------
+// pyrDown: 5x5 [1 4 6 4 1]^2 / 256, BORDER_REFLECT_101, (sum+128)>>8.
+// Reference: src/pyrdown.cu:16-52.  One block computes a 32x8 output tile
+// from a shared 67x19 source tile (coalesced row loads, reflected indices
+// resolved once at load time).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int reflect101(int i, int n)
+{
+    if (i < 0) i = -i;
+    if (i >= n) i = 2 * n - 2 - i;
+    return i < 0 ? 0 : i;
+}
+
+constexpr int kPdTx = 32, kPdTy = 8;
+constexpr int kPdSw = 2 * kPdTx + 3, kPdSh = 2 * kPdTy + 3;
+
+template <int NB>
+__global__ void __launch_bounds__(256) k_pyrdown(const __grid_constant__ PyrDownBatch<NB> b)
+{
+    const PyrDownDesc& P = b.d[blockIdx.z];
+    const int x0 = blockIdx.x * kPdTx, y0 = blockIdx.y * kPdTy;
+    if (x0 >= P.dw || y0 >= P.dh) return;
+    __shared__ uint8_t tile[kPdSh][kPdSw + 1];
+    const int sx0 = 2 * x0 - 2, sy0 = 2 * y0 - 2;
+    for (int i = threadIdx.x; i < kPdSh * kPdSw; i += blockDim.x) {
+        const int r = i / kPdSw, c = i - r * kPdSw;
+        const int sy = reflect101(sy0 + r, P.sh), sx = reflect101(sx0 + c, P.sw);
+        tile[r][c] = P.src[(size_t)sy * P.sstep + sx];
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & (kPdTx - 1), ty = threadIdx.x / kPdTx;
+    const int x = x0 + tx, y = y0 + ty;
+    if (x >= P.dw || y >= P.dh) return;
+    const int w5[5] = {1, 4, 6, 4, 1};
+    int sum = 0;
+#pragma unroll
+    for (int ky = 0; ky < 5; ++ky) {
+        int rs = 0;
+#pragma unroll
+        for (int kx = 0; kx < 5; ++kx) rs += w5[kx] * (int)tile[2 * ty + ky][2 * tx + kx];
+        sum += w5[ky] * rs;
+    }
+    P.dst[(size_t)y * P.dstep + x] = (uint8_t)((sum + 128) >> 8);
+}
+
+// ---------------------------------------------------------------------------
+// Features.  Census: 5x5, replicate borders, MSB first, dy-major, bit =
+// neighbour < centre (src/sgm_kernels.cu:251-298).  BT: the Sobel-like
+// x-gradient clipped to +-ftzero and offset by ftzero
+// (src/sgm_kernels.cu:94-118), plus for both the gradient and intensity
+// channels the half-sample interval [lo, hi] of dev_bt_channel_cost
+// (src/sgm_kernels.cu:1002-1028) with clamped neighbours, packed as
+// v | lo<<8 | hi<<16.
+// ---------------------------------------------------------------------------
+constexpr int kFtX = 32, kFtY = 8, kFtHalo = 2;
+constexpr int kFtW = kFtX + 2 * kFtHalo, kFtH = kFtY + 2 * kFtHalo;
+
+template <int NJ>
+__global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<NJ> jobs)
+{
+    const LevelDesc& J = jobs.d[blockIdx.z >> 1];
+    const int view = blockIdx.z & 1;
+    const int x0 = blockIdx.x * kFtX, y0 = blockIdx.y * kFtY;
+    if (x0 >= J.w || y0 >= J.h) return;
+    const uint8_t* img = view ? J.right : J.left;
+    const int step = view ? J.rstep : J.lstep;
+    uint2* feat = view ? J.featR : J.featL;
+    const int W = J.w, H = J.h;
+
+    __shared__ uint8_t t[kFtH][kFtW];
+    for (int i = threadIdx.x; i < kFtH * kFtW; i += blockDim.x) {
+        const int r = i / kFtW, c = i - r * kFtW;
+        t[r][c] = img[(size_t)iclamp(y0 - kFtHalo + r, 0, H - 1) * step + iclamp(x0 - kFtHalo + c, 0, W - 1)];
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & (kFtX - 1), ty = threadIdx.x / kFtX;
+    const int x = x0 + tx, y = y0 + ty;
+    if (x >= W || y >= H) return;
+    // pixel (gy, gx), both already clamped to the image
+    auto px = [&](int gy, int gx) -> int { return t[gy - y0 + kFtHalo][gx - x0 + kFtHalo]; };
+    uint2 f;
+    if (J.cost == COST_CENSUS) {
+        const int c = px(y, x);
+        uint32_t cv = 0;
+#pragma unroll
+        for (int dy = 0; dy < 5; ++dy) {
+            const int gy = iclamp(y + dy - 2, 0, H - 1);
+#pragma unroll
+            for (int dx = 0; dx < 5; ++dx) {
+                cv <<= 1;
+                cv |= (uint32_t)(px(gy, iclamp(x + dx - 2, 0, W - 1)) < c);
+            }
+        }
+        f = make_uint2(cv, 0u);
+    } else {
+        const int ftzero = imax(J.pfc, 15) | 1;
+        const int yp = imax(y - 1, 0), yn = imin(y + 1, H - 1);
+        auto grad = [&](int gx) -> int {
+            const int xp = imax(gx - 1, 0), xn = imin(gx + 1, W - 1);
+            int g = (px(y, xn) - px(y, xp)) * 2;
+            g += px(yp, xn) - px(yp, xp);
+            g += px(yn, xn) - px(yn, xp);
+            return iclamp(g, -ftzero, ftzero) + ftzero;
+        };
+        auto interval = [](int v, int l, int r) -> uint32_t {
+            const int vl = (v + l) / 2, vr = (v + r) / 2;
+            const int lo = imin(imin(vl, vr), v), hi = imax(imax(vl, vr), v);
+            return (uint32_t)v | ((uint32_t)lo << 8) | ((uint32_t)hi << 16);
+        };
+        const int xm = imax(x - 1, 0), xq = imin(x + 1, W - 1);
+        f.x = interval(grad(x), grad(xm), grad(xq));
+        f.y = interval(px(y, x), px(y, xm), px(y, xq));
+    }
+    feat[(size_t)y * W + x] = f;
+}
+
+// ---------------------------------------------------------------------------
+// Refine labels: kernel_PrepareRefineLabels, src/sgm_kernels.cu:955-1000.
+// A rejected parent (invalid disparity or confidence below the minimum)
+// becomes kNoParent: every label of the pixel is invalid (valid_mask = 0).
+// ---------------------------------------------------------------------------
+template <int NJ>
+__global__ void __launch_bounds__(256) k_refine_labels(const __grid_constant__ Jobs<NJ> jobs)
+{
+    const LevelDesc& J = jobs.d[blockIdx.z];
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= J.w || y >= J.h) return;
+    const int px = imin(x >> 1, J.pw - 1), py = imin(y >> 1, J.ph - 1);
+    const int16_t raw = J.pdisp[(size_t)py * J.pd_pitch + px];
+    const float conf = J.pconf[(size_t)py * J.pc_pitch + px];
+    const int16_t pinv = (int16_t)((J.minD - 1) * 16);
+    int16_t out = kNoParent;
+    if (!(raw == pinv || conf < J.minConf)) {
+        const int pred16 = (int)raw * 2;
+        const int center = (pred16 + 8) >> 4;
+        const int resid = pred16 - center * 16;
+        int base = center + (resid < 0 ? -(J.D / 2) : -(J.D / 2) + 1);
+        const int physMax = imin(J.maxD, x);
+        const int largest = physMax - J.D + 1;
+        base = largest >= J.minD ? imin(imax(base, J.minD), largest) : J.minD;
+        out = (int16_t)base;
+    }
+    J.base[(size_t)y * J.w + x] = out;
+}
+
+// ---------------------------------------------------------------------------
+// Adaptive P2 table.  dev_adaptive_p2 (src/sgm_kernels.cu:63-74) depends on
+// the pixels only through |I(p) - I(p-r)| in [0, 255]; the table holds its
+// value for every difference, computed on the device with the same
+// expression and the same intrinsic (__expf) so that each entry equals the
+// reference's per-voxel value.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ int adaptive_p2_value(int P2, int cur, int prev, float alpha, float beta,
+                                              float lowerMult, float upperMult)
+{
+    const float diff = fabsf((float)(cur - prev));
+    const float ratio = lowerMult + (1.0f + alpha - lowerMult) * __expf(-diff / beta);
+    float adaptive = (float)P2 * ratio;
+    const float lower = fmaxf(1.0f, (float)P2 * lowerMult);
+    const float upper = (float)P2 * upperMult;
+    adaptive = fminf(upper, fmaxf(lower, adaptive));
+    return (int)(adaptive + 0.5f);
+}
+
+__global__ void k_p2_table(int* lut, int P2, float alpha, float beta, float lower, float upper)
+{
+    const int i = threadIdx.x;
+    if (i < 256) lut[i] = adaptive_p2_value(P2, i, 0, alpha, beta, lower, upper);
+}
+
+// ---------------------------------------------------------------------------
+// Census cost volume.  Coarse / single-scale: kernel_CensusCost
+// (src/sgm_kernels.cu:303-327), 24 when x - d - minD is outside the image.
+// Refine: kernel_CensusCostLocal (src/sgm_kernels.cu:1112-1133), kMax for a
+// geometry-invalid label.  Each thread writes two labels (one 32-bit store).
+// ---------------------------------------------------------------------------
+template <int NJ>
+__global__ void __launch_bounds__(256) k_cost_census(const __grid_constant__ Jobs<NJ> jobs)
+{
+    const LevelDesc& J = jobs.d[blockIdx.y];
+    const int half = J.D >> 1;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)J.w * J.h * half;
+    if (i >= total) return;
+    const int pair = (int)(i % half);
+    const long long p = i / half;
+    const int y = (int)(p / J.w), x = (int)(p - (long long)y * J.w);
+    const uint32_t cl = J.featL[p].x;
+    const uint2* rrow = J.featR + (size_t)y * J.w;
+    int c[2];
+    if (J.refine) {
+        const int base = J.base[p];
+        int lo, hi;
+        label_range(J, x, base, lo, hi);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int d = 2 * pair + k;
+            c[k] = (d >= lo && d <= hi) ? __popc(cl ^ rrow[x - (base + d)].x) : kMax;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int x2 = x - (2 * pair + k + J.minD);
+            c[k] = (x2 >= 0 && x2 < J.w) ? __popc(cl ^ rrow[x2].x) : 24;
+        }
+    }
+    reinterpret_cast<uint32_t*>(J.C + p * J.D)[pair] = (uint32_t)(uint16_t)c[0] | ((uint32_t)(uint16_t)c[1] << 16);
+}
+
+// BT cost of one (left pixel, right pixel) pair from packed features:
+// dev_bt_pixel_cost, src/sgm_kernels.cu:1030-1043.
+__device__ __forceinline__ int bt_channel(uint32_t a, uint32_t b)
+{
+    const int u = a & 255, u0 = (a >> 8) & 255, u1 = (a >> 16) & 255;
+    const int v = b & 255, v0 = (b >> 8) & 255, v1 = (b >> 16) & 255;
+    const int c0 = imax(imax(0, u - v1), v0 - u);
+    const int c1 = imax(imax(0, v - u1), u0 - v);
+    return imin(c0, c1);
+}
+
+__device__ __forceinline__ int bt_pixel(uint2 l, uint2 r)
+{
+    return imin(255, bt_channel(l.x, r.x) + (bt_channel(l.y, r.y) >> 2));
+}
+
+// ---------------------------------------------------------------------------
+// BT coarse / single-scale cost: kernel_BTCost followed by kernel_BoxFilterH
+// and kernel_BoxFilterV (src/sgm_kernels.cu:139-239, 354-416), fused.  The
+// separable sums keep the reference's two saturation points:
+//   C = min(MAX, sum_dy min(MAX, sum_dx bt(clamp(y+dy), clamp(x+dx), d))).
+// One block: 32 x 8 output pixels x 16 labels.  bt values are staged in
+// shared memory for the (8+2h) x (32+2h) window of clamped pixels.
+// ---------------------------------------------------------------------------
+constexpr int kBxX = 32, kBxY = 8, kBxD = 16;
+
+template <int NJ>
+__global__ void __launch_bounds__(256) k_cost_bt_box(const __grid_constant__ Jobs<NJ> jobs, int maxHalf, int nxt)
+{
+    const LevelDesc& J = jobs.d[blockIdx.z];
+    const int x0 = (blockIdx.x % nxt) * kBxX;
+    const int d0 = (blockIdx.x / nxt) * kBxD;
+    const int y0 = blockIdx.y * kBxY;
+    if (x0 >= J.w || y0 >= J.h || d0 >= J.D) return;
+    const int h = J.bs / 2;
+    const int SW = kBxX + 2 * maxHalf, SH = kBxY + 2 * maxHalf;
+    extern __shared__ unsigned char sm[];
+    uint8_t* bt = sm;                                               // [SH][SW][kBxD]
+    uint16_t* hs = reinterpret_cast<uint16_t*>(sm + ((SH * SW * kBxD + 15) & ~15));  // [SH][kBxX][kBxD]
+    const int W = J.w, H = J.h;
+    const int sw = kBxX + 2 * h, sh = kBxY + 2 * h;
+    for (int i = threadIdx.x; i < sh * sw * kBxD; i += blockDim.x) {
+        const int dd = i % kBxD;
+        const int j = (i / kBxD) % sw;
+        const int r = i / (kBxD * sw);
+        const int gy = iclamp(y0 - h + r, 0, H - 1), gx = iclamp(x0 - h + j, 0, W - 1);
+        const int x2 = gx - (d0 + dd + J.minD);
+        int v = 255;
+        if (x2 >= 0 && x2 < W) v = bt_pixel(J.featL[(size_t)gy * W + gx], J.featR[(size_t)gy * W + x2]);
+        bt[(r * SW + j) * kBxD + dd] = (uint8_t)v;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < sh * kBxX * kBxD; i += blockDim.x) {
+        const int dd = i % kBxD;
+        const int j = (i / kBxD) % kBxX;
+        const int r = i / (kBxD * kBxX);
+        int s = 0;
+        for (int k = 0; k <= 2 * h; ++k) s += bt[(r * SW + j + k) * kBxD + dd];
+        hs[(r * kBxX + j) * kBxD + dd] = (uint16_t)imin(kMax, s);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBxY * kBxX * (kBxD / 2); i += blockDim.x) {
+        const int dp = i % (kBxD / 2);
+        const int j = (i / (kBxD / 2)) % kBxX;
+        const int r = i / ((kBxD / 2) * kBxX);
+        const int x = x0 + j, y = y0 + r;
+        if (x >= W || y >= H) continue;
+        int s0 = 0, s1 = 0;
+        for (int k = 0; k <= 2 * h; ++k) {
+            s0 += hs[((r + k) * kBxX + j) * kBxD + 2 * dp];
+            s1 += hs[((r + k) * kBxX + j) * kBxD + 2 * dp + 1];
+        }
+        const uint32_t v = (uint32_t)imin(kMax, s0) | ((uint32_t)imin(kMax, s1) << 16);
+        reinterpret_cast<uint32_t*>(J.C + ((size_t)y * W + x) * J.D + d0)[dp] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// BT refine cost: kernel_BTWindowCostLocal, src/sgm_kernels.cu:1075-1110.
+// Direct blockSize^2 window of BT pixel costs at the real disparity
+// base + d over clamped pixels; kMax for a geometry-invalid label; the sum
+// is clamped to kMax - 1.  One thread per (pixel, label).
+// ---------------------------------------------------------------------------
+template <int NJ>
+__global__ void __launch_bounds__(256) k_cost_bt_local(const __grid_constant__ Jobs<NJ> jobs)
+{
+    const LevelDesc& J = jobs.d[blockIdx.y];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)J.w * J.h * J.D;
+    if (i >= total) return;
+    const int d = (int)(i % J.D);
+    const long long p = i / J.D;
+    const int y = (int)(p / J.w), x = (int)(p - (long long)y * J.w);
+    const int base = J.base[p];
+    int lo, hi;
+    label_range(J, x, base, lo, hi);
+    int out = kMax;
+    if (d >= lo && d <= hi) {
+        const int real = base + d, half = J.bs / 2, W = J.w, H = J.h;
+        int sum = 0;
+        for (int dy = -half; dy <= half; ++dy) {
+            const int yy = iclamp(y + dy, 0, H - 1);
+            const uint2* lrow = J.featL + (size_t)yy * W;
+            const uint2* rrow = J.featR + (size_t)yy * W;
+            for (int dx = -half; dx <= half; ++dx) {
+                const int xx = iclamp(x + dx, 0, W - 1);
+                const int x2 = xx - real;
+                sum += (x2 >= 0 && x2 < W) ? bt_pixel(__ldg(&lrow[xx]), __ldg(&rrow[x2])) : 255;
+            }
+        }
+        out = imin(sum, kMax - 1);
+    }
+    J.C[i] = (int16_t)out;
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+template <int NB>
+cudaError_t launch_pyrdown(const PyrDownBatch<NB>& b, int max_dw, int max_dh, cudaStream_t st)
+{
+    dim3 grid((max_dw + kPdTx - 1) / kPdTx, (max_dh + kPdTy - 1) / kPdTy, b.n);
+    k_pyrdown<NB><<<grid, 256, 0, st>>>(b);
+    return cudaGetLastError();
+}
+template cudaError_t launch_pyrdown<1>(const PyrDownBatch<1>&, int, int, cudaStream_t);
+template cudaError_t launch_pyrdown<2>(const PyrDownBatch<2>&, int, int, cudaStream_t);
+template cudaError_t launch_pyrdown<kBatchPyr>(const PyrDownBatch<kBatchPyr>&, int, int, cudaStream_t);
+
+cudaError_t launch_p2_table(int* lut, int P2, float alpha, float beta, float lower, float upper, cudaStream_t st)
+{
+    k_p2_table<<<1, 256, 0, st>>>(lut, P2, alpha, beta, lower, upper);
+    return cudaGetLastError();
+}
+
+template <int NJ>
+cudaError_t launch_prepare(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
+{
+    dim3 gf((e.max_w + kFtX - 1) / kFtX, (e.max_h + kFtY - 1) / kFtY, 2 * jobs.n);
+    k_features<NJ><<<gf, 256, 0, st>>>(jobs);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    if (e.any_refine) {
+        dim3 gl((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
+        k_refine_labels<NJ><<<gl, 256, 0, st>>>(jobs);
+        err = cudaGetLastError();
+    }
+    return err;
+}
+
+// All jobs in `jobs` share the cost mode and the refine flag.
+template <int NJ>
+cudaError_t launch_cost(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
+{
+    const LevelDesc& J0 = jobs.d[0];
+    if (J0.cost == COST_CENSUS) {
+        const long long n = e.max_vox / 2;
+        dim3 g((unsigned)((n + 255) / 256), jobs.n);
+        k_cost_census<NJ><<<g, 256, 0, st>>>(jobs);
+    } else if (J0.refine) {
+        dim3 g((unsigned)((e.max_vox + 255) / 256), jobs.n);
+        k_cost_bt_local<NJ><<<g, 256, 0, st>>>(jobs);
+    } else {
+        int maxHalf = 0;
+        for (int j = 0; j < jobs.n; ++j) maxHalf = std::max(maxHalf, jobs.d[j].bs / 2);
+        const int SW = kBxX + 2 * maxHalf, SH = kBxY + 2 * maxHalf;
+        const size_t smem = ((SH * SW * kBxD + 15) & ~15) + (size_t)SH * kBxX * kBxD * 2;
+        if (smem > 48 * 1024) {
+            cudaError_t err = cudaFuncSetAttribute(k_cost_bt_box<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+            if (err != cudaSuccess) return err;
+        }
+        const int nxt = (e.max_w + kBxX - 1) / kBxX;
+        dim3 g(nxt * ((e.max_D + kBxD - 1) / kBxD), (e.max_h + kBxY - 1) / kBxY, jobs.n);
+        k_cost_bt_box<NJ><<<g, 256, smem, st>>>(jobs, maxHalf, nxt);
+    }
+    return cudaGetLastError();
+}
+
+#define PG_INST(NJ)                                                                          \
+    template cudaError_t launch_prepare<NJ>(const Jobs<NJ>&, const LevelExtent&, cudaStream_t); \
+    template cudaError_t launch_cost<NJ>(const Jobs<NJ>&, const LevelExtent&, cudaStream_t);
+PG_INST(1)
+PG_INST(kBatchJobs)
+#undef PG_INST
+
+}  // namespace pg

@@ -1,0 +1,9 @@
+// k_paths_ss.cu -- single-scale instantiations of the aggregation kernels.
+#include "k_paths.cuh"
+
+namespace pg {
+
+template cudaError_t launch_paths_mode<false, 1>(const Jobs<1>&, const LevelExtent&, cudaStream_t);
+template cudaError_t launch_paths_mode<false, kBatchJobs>(const Jobs<kBatchJobs>&, const LevelExtent&, cudaStream_t);
+
+}  // namespace pg

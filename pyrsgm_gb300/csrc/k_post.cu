@@ -1,0 +1,89 @@
+// k_post.cu -- 3x3 median, median-changed confidence reset and the output
+// conversion of one level, fused into one pass; plus the path-kernel
+// dispatch.  Reference: kernel_MedianFilter3x3, kernel_ClearChangedMedian-
+// Confidence (src/sgm_kernels.cu:891-931), convertDispAndConfKernel
+// (src/sgm_kernels.cu:1530-1551) and the output copies of
+// pyrsgm_compute_level / pyrsgm_compute_single_scale
+// (src/sgm_kernels.cu:1837-1858, 2053-2069).
+#include "sgm_common.cuh"
+#include "sgm_launch.h"
+
+namespace pg {
+
+template <bool PYR, int NJ>
+cudaError_t launch_paths_mode(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st);
+
+PathShape path_shape(int D)
+{
+    if (D <= 16) return {16, 1};
+    if (D <= 32) return {32, 1};
+    int k = 2;
+    while (32 * k < D) k *= 2;
+    return {32, k};
+}
+
+template <int NJ>
+cudaError_t launch_paths(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
+{
+    return jobs.d[0].pyr ? launch_paths_mode<true, NJ>(jobs, e, st) : launch_paths_mode<false, NJ>(jobs, e, st);
+}
+
+template <int NJ>
+__global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> jobs)
+{
+    const LevelDesc& J = jobs.d[blockIdx.z];
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= J.w || y >= J.h) return;
+    const int W = J.w, H = J.h;
+    const size_t p = (size_t)y * W + x;
+    int d = J.disp_raw[p];
+    float c = J.conf_raw[p];
+    if (J.post & POST_MEDIAN) {
+        int v[9];
+        int n = 0;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int yy = y + dy;
+            if (yy < 0 || yy >= H) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int xx = x + dx;
+                if (xx < 0 || xx >= W) continue;
+                v[n++] = J.disp_raw[(size_t)yy * W + xx];
+            }
+        }
+        for (int i = 1; i < n; ++i) {
+            const int key = v[i];
+            int j = i - 1;
+            while (j >= 0 && v[j] > key) { v[j + 1] = v[j]; --j; }
+            v[j + 1] = key;
+        }
+        const int m = v[n / 2];
+        if (m != d) c = 0.0f;
+        d = m;
+    }
+    if (J.out16) J.out16[(size_t)y * J.out16_pitch + x] = (int16_t)d;
+    if (J.out32 && J.outc) {
+        const int16_t inv = (int16_t)((J.minD - 1) * 16);
+        const float f = (int16_t)d / 16.0f;
+        const bool ok = (int16_t)d != inv && f > 0.0f;
+        J.out32[(size_t)y * J.out32_pitch + x] = ok ? f : 0.0f;
+        J.outc[(size_t)y * J.outc_pitch + x] = ok ? c : 0.0f;
+    } else if (J.outc && J.conf_only_copy) {
+        J.outc[(size_t)y * J.outc_pitch + x] = c;
+    }
+}
+
+template <int NJ>
+cudaError_t launch_post(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
+{
+    dim3 g((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
+    k_post<NJ><<<g, 256, 0, st>>>(jobs);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_paths<1>(const Jobs<1>&, const LevelExtent&, cudaStream_t);
+template cudaError_t launch_paths<kBatchJobs>(const Jobs<kBatchJobs>&, const LevelExtent&, cudaStream_t);
+template cudaError_t launch_post<1>(const Jobs<1>&, const LevelExtent&, cudaStream_t);
+template cudaError_t launch_post<kBatchJobs>(const Jobs<kBatchJobs>&, const LevelExtent&, cudaStream_t);
+
+}  // namespace pg

@@ -1,0 +1,76 @@
+// sgm_launch.h -- host-side launch interface of the pyrsgm-gb300 kernels.
+//
+// Every stage is launched for a batch of independent level jobs (one stereo
+// pair's level each); a single-pair call is a batch of one.  Job
+// descriptors travel by value in the kernel parameter block, so a launch
+// needs no host-to-device copy and can be captured in a CUDA graph.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "sgm_common.cuh"
+
+namespace pg {
+
+constexpr int kBatchJobs = 16;  // level jobs per batched launch
+constexpr int kBatchPyr = 32;   // pyrDown images per batched launch
+
+struct PyrDownDesc {
+    const uint8_t* src;
+    uint8_t* dst;
+    int sstep, sw, sh, dstep, dw, dh;
+};
+
+template <int NB>
+struct PyrDownBatch {
+    PyrDownDesc d[NB];
+    int n;
+};
+
+// Largest extents over the jobs of one launch (grid sizing).
+struct LevelExtent {
+    int max_w = 0, max_h = 0, max_D = 0;
+    long long max_vox = 0;
+    bool any_refine = false;
+};
+
+template <int NJ>
+LevelExtent extent_of(const Jobs<NJ>& j)
+{
+    LevelExtent e;
+    for (int i = 0; i < j.n; ++i) {
+        const LevelDesc& d = j.d[i];
+        e.max_w = std::max(e.max_w, d.w);
+        e.max_h = std::max(e.max_h, d.h);
+        e.max_D = std::max(e.max_D, d.D);
+        e.max_vox = std::max(e.max_vox, (long long)d.w * d.h * d.D);
+        e.any_refine = e.any_refine || d.refine;
+    }
+    return e;
+}
+
+// Aggregation kernel variant: G lanes per path chain, K labels per lane,
+// G*K >= D (padding labels behave as permanently invalid).
+struct PathShape {
+    int G, K;
+};
+PathShape path_shape(int D);
+
+template <int NB>
+cudaError_t launch_pyrdown(const PyrDownBatch<NB>& b, int max_dw, int max_dh, cudaStream_t st);
+cudaError_t launch_p2_table(int* lut, int P2, float alpha, float beta, float lower, float upper,
+                            cudaStream_t st);
+template <int NJ>
+cudaError_t launch_prepare(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st);
+template <int NJ>
+cudaError_t launch_cost(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st);
+// All jobs in one call share pyr (mode) and the path shape of their D.
+template <int NJ>
+cudaError_t launch_paths(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st);
+template <int NJ>
+cudaError_t launch_post(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st);
+
+}  // namespace pg

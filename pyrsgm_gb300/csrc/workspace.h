@@ -1,0 +1,48 @@
+// workspace.h -- device buffers of one level geometry (the opaque object
+// behind pyrsgm_create_workspace).  One cudaMalloc, carved into:
+//   featL, featR  uint2  [h][w]     census bits or BT sample intervals
+//   base          int16  [h][w]     refine label base (kNoParent = rejected)
+//   C             int16  [h][w][D]  matching cost
+//   V             int16  [h][w][D]  aggregation volume
+//   disp_raw      int16  [h][w]     disparity*16 before the median
+//   conf_raw      float  [h][w]     confidence before the median reset
+//   lut           int    [256]      adaptive-P2 table
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "sgm_common.cuh"
+
+namespace pg {
+
+struct Workspace {
+    int width = 0, height = 0, disp = 0;
+    void* mem = nullptr;
+    size_t bytes = 0;
+    bool owned = false;
+    int debug = 0;
+    uint2* featL = nullptr;
+    uint2* featR = nullptr;
+    int16_t* base = nullptr;
+    int16_t* C = nullptr;
+    int16_t* V = nullptr;
+    int16_t* disp_raw = nullptr;
+    float* conf_raw = nullptr;
+    int* lut = nullptr;
+
+    static size_t bytes_for(int w, int h, int D);
+    // Lay the buffers of a (w, h, D) geometry out from `p` (bytes_for bytes).
+    void carve(unsigned char* p, int w, int h, int D);
+    int ensure(int w, int h, int D);
+    void release();
+};
+
+void sanitize_p2(int& adaptive, float& alpha, float& beta, float& lower, float& upper);
+void fill_workspace_ptrs(LevelDesc& d, const Workspace& ws);
+int run_level_single(const LevelDesc& d, cudaStream_t st, float alpha, float beta, float lower, float upper,
+                     const char* what);
+
+}  // namespace pg

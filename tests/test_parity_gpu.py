@@ -1,0 +1,83 @@
+"""Parity on the GPU: the CUDA library against the CPU oracle and against the
+reference's own kernels (run from oracle/_ref through the harness), on the
+same seeded inputs.  Integer outputs (disparity x16, cost volume, aggregated
+volume) must match bit for bit; disp32 and confidence within 1e-6 absolute.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests import _oracle, _runners, cases
+
+pytestmark = pytest.mark.gpu
+
+ALL_CASES = cases.SINGLE_SCALE + cases.LEVELS + cases.MATCHER
+IDS = [c["name"] for c in ALL_CASES]
+
+
+@pytest.mark.parametrize("case", ALL_CASES, ids=IDS)
+def test_cuda_matches_oracle(case):
+    lut = _runners.device_lut(case)
+    mine = _runners.run_mine(case)
+    orc = _runners.run_oracle(case, lut)
+    bad = _runners.compare(mine, orc)
+    assert not bad, bad
+
+
+def _need_ref():
+    if not _oracle.ref_available():
+        pytest.fail("reference kernels (oracle/_ref/*.fatbin + harness) are not available")
+
+
+@pytest.mark.parametrize("case", ALL_CASES, ids=IDS)
+def test_cuda_matches_reference_kernels(case):
+    _need_ref()
+    mine = _runners.run_mine(case)
+    ref = _runners.run_ref(case)
+    bad = _runners.compare(mine, ref)
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("case", ALL_CASES, ids=IDS)
+def test_oracle_matches_reference_kernels(case):
+    _need_ref()
+    lut = _runners.device_lut(case)
+    orc = _runners.run_oracle(case, lut)
+    ref = _runners.run_ref(case)
+    bad = _runners.compare(orc, ref)
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("w,h", cases.PYRDOWN)
+def test_pyrdown_matches_reference(w, h):
+    import torch
+    import pyrsgm_gb300 as pg
+    src = cases.pyrdown_input(w, h)
+    mine = pg.pyrdown(torch.from_numpy(src).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(mine, _oracle.orc_pyrdown(src))
+    if _oracle.ref_available():
+        np.testing.assert_array_equal(mine, _runners.run_ref_pyrdown(src))
+
+
+def test_pyrdown_pitched_views():
+    """Pitched (strided) source and destination, as from cudaMallocPitch."""
+    import torch
+    import pyrsgm_gb300 as pg
+    src = cases.pyrdown_input(97, 48)
+    big = torch.zeros((48, 128), dtype=torch.uint8, device="cuda")
+    big[:, :97] = torch.from_numpy(src).cuda()
+    dst_big = torch.zeros((24, 64), dtype=torch.uint8, device="cuda")
+    pg.pyrdown(big[:, :97], dst_big[:, :49])
+    np.testing.assert_array_equal(dst_big[:, :49].cpu().numpy(), _oracle.orc_pyrdown(src))
+    assert int(dst_big[:, 49:].abs().sum()) == 0
+
+
+def test_p2_table_matches_libm_closely():
+    """The device table uses __expf; libm expf may round differently near .5,
+    but never by more than one P2 step."""
+    for P2, a in ((2400, cases.P2_DEFAULT), (32, cases.P2_SMOKE), (800, (0.0, 5.0, 0.2, 1.0))):
+        case = dict(kind="ss", adaptive=True, P2=P2, p2p=a)
+        dev = _runners.device_lut(case)
+        host = _oracle.p2_table_libm(P2, *a)
+        assert np.max(np.abs(dev.astype(np.int64) - host)) <= 1
