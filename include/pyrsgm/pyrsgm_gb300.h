@@ -75,6 +75,18 @@ size_t pyrsgm_gb300_matcher_device_bytes(void* matcher);
 
 const char* pyrsgm_gb300_version(void);
 
+/* Kernel launches issued by this library since the process started. */
+unsigned long long pyrsgm_gb300_launch_count(void);
+
+/* Per-kernel profiling with CUDA events recorded on each launch's stream.
+ * pyrsgm_gb300_profile(1) clears the records and starts recording,
+ * pyrsgm_gb300_profile(0) stops.  _read() waits for the recorded events of
+ * one kernel kind (0 pyrDown, 1 features, 2 refine labels, 3 cost volume,
+ * 4 top->bottom path, 5 row pass, 6 post, 7 P2 table) and returns the summed
+ * device time in ms, the launch count and the summed algorithmic bytes. */
+int pyrsgm_gb300_profile(int enable);
+int pyrsgm_gb300_profile_read(int kind, double* ms_total, long long* launches, double* bytes_total);
+
 #ifdef __cplusplus
 }
 #endif

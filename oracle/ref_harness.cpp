@@ -47,17 +47,28 @@ cudaKernel_t g_k[K_COUNT] = {};
 bool g_ready = false;
 char g_err[512] = "ref harness not initialised";
 
-// Matches "<len><name>" inside an Itanium-mangled name, or the exact name for
-// the one kernel with C linkage (convertDispAndConfKernel).
-bool nameMatches(const char* mangled, const char* name)
+// Unqualified function name of an Itanium-mangled symbol: "_Z<len><id>..."
+// or "_ZN<len><id>...<len><id>E..." (the last component); a name without
+// the _Z prefix (C linkage) is returned as is.
+std::string baseName(const char* m)
 {
-    if (std::strcmp(mangled, name) == 0) return true;
-    std::string key = std::to_string(std::strlen(name)) + name;
-    const char* hit = std::strstr(mangled, key.c_str());
-    if (!hit) return false;
-    // the length prefix must not be the tail of a longer number
-    return hit == mangled || !(hit[-1] >= '0' && hit[-1] <= '9');
+    if (std::strncmp(m, "_Z", 2) != 0) return m;
+    const char* p = m + 2;
+    const bool nested = *p == 'N';
+    if (nested) ++p;
+    std::string last;
+    while (*p >= '0' && *p <= '9') {
+        size_t len = 0;
+        while (*p >= '0' && *p <= '9') len = len * 10 + (size_t)(*p++ - '0');
+        if (std::strlen(p) < len) return "";
+        last.assign(p, len);
+        p += len;
+        if (!nested) break;
+    }
+    return last;
 }
+
+bool nameMatches(const char* mangled, const char* name) { return baseName(mangled) == name; }
 
 bool loadLibrary(const char* path)
 {

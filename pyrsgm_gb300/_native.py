@@ -59,6 +59,9 @@ _SIGS = {
     "pyrsgm_gb300_level_geometry": (_i, [_i, _i, C.POINTER(Params), C.POINTER(_i), C.c_char_p, _sz]),
     "pyrsgm_gb300_matcher_device_bytes": (_sz, [_vp]),
     "pyrsgm_gb300_version": (C.c_char_p, []),
+    "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
+    "pyrsgm_gb300_profile": (_i, [_i]),
+    "pyrsgm_gb300_profile_read": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
 }
 
 # Entry points declared in include/pyrsgm/*.h (checked by the tests).

@@ -42,7 +42,7 @@ def _sources() -> list[str]:
 
 
 def _flags() -> list[str]:
-    return ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
+    return ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-Wall,-Wextra,-Wno-unused-parameter",
                    "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
 
 
@@ -56,6 +56,8 @@ def _compile(src: str, hdr_mtime: float, verbose: bool) -> str:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout.strip() or r.stderr.strip()):
+        print(r.stdout + r.stderr, flush=True)
     return obj
 
 

@@ -7,6 +7,7 @@
 // (T->B) -> row pass (L->R + R->L + WTA + disp2 + LR check) -> median and
 // outputs, 4-6 launches per level instead of ~17.
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -19,6 +20,9 @@
 #include "workspace.h"
 
 namespace pg {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
@@ -322,5 +326,7 @@ int pyrsgm_gb300_p2_table(int* d_table, int P2, float p2Alpha, float p2Beta, flo
 }
 
 const char* pyrsgm_gb300_version(void) { return "0.1.0-gb300"; }
+
+unsigned long long pyrsgm_gb300_launch_count(void) { return pg::g_launches.load(std::memory_order_relaxed); }
 
 }  // extern "C"

@@ -2,6 +2,7 @@
 // refine-label preparation, the adaptive-P2 table and the matching-cost
 // volume.  Integer arithmetic, clamps and sentinels follow the reference
 // kernels cited at each function (reference file:line).
+#include "profiler.h"
 #include "sgm_common.cuh"
 #include "sgm_launch.h"
 
@@ -339,7 +340,14 @@ template <int NB>
 cudaError_t launch_pyrdown(const PyrDownBatch<NB>& b, int max_dw, int max_dh, cudaStream_t st)
 {
     dim3 grid((max_dw + kPdTx - 1) / kPdTx, (max_dh + kPdTy - 1) / kPdTy, b.n);
+    prof_begin(st);
     k_pyrdown<NB><<<grid, 256, 0, st>>>(b);
+    count_launch();
+    if (prof_enabled()) {
+        double by = 0;
+        for (int i = 0; i < b.n; ++i) by += (double)b.d[i].sw * b.d[i].sh + (double)b.d[i].dw * b.d[i].dh;
+        prof_end(PK_PYRDOWN, by, st);
+    }
     return cudaGetLastError();
 }
 template cudaError_t launch_pyrdown<1>(const PyrDownBatch<1>&, int, int, cudaStream_t);
@@ -348,7 +356,10 @@ template cudaError_t launch_pyrdown<kBatchPyr>(const PyrDownBatch<kBatchPyr>&, i
 
 cudaError_t launch_p2_table(int* lut, int P2, float alpha, float beta, float lower, float upper, cudaStream_t st)
 {
+    prof_begin(st);
     k_p2_table<<<1, 256, 0, st>>>(lut, P2, alpha, beta, lower, upper);
+    count_launch();
+    prof_end(PK_P2TABLE, 1024.0, st);
     return cudaGetLastError();
 }
 
@@ -356,12 +367,18 @@ template <int NJ>
 cudaError_t launch_prepare(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
     dim3 gf((e.max_w + kFtX - 1) / kFtX, (e.max_h + kFtY - 1) / kFtY, 2 * jobs.n);
+    prof_begin(st);
     k_features<NJ><<<gf, 256, 0, st>>>(jobs);
+    count_launch();
+    prof_end(PK_FEATURES, jobs_px(jobs) * 2 * (1 + 8), st);  // read u8, write uint2, both views
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     if (e.any_refine) {
         dim3 gl((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
+        prof_begin(st);
         k_refine_labels<NJ><<<gl, 256, 0, st>>>(jobs);
+        count_launch();
+        prof_end(PK_LABELS, jobs_px(jobs) * (2 + 6.0 / 4), st);  // write base, read the 1/4-size parent
         err = cudaGetLastError();
     }
     return err;
@@ -372,6 +389,7 @@ template <int NJ>
 cudaError_t launch_cost(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
     const LevelDesc& J0 = jobs.d[0];
+    prof_begin(st);
     if (J0.cost == COST_CENSUS) {
         const long long n = e.max_vox / 2;
         dim3 g((unsigned)((n + 255) / 256), jobs.n);
@@ -393,6 +411,9 @@ cudaError_t launch_cost(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t
         dim3 g(nxt * ((e.max_D + kBxD - 1) / kBxD), (e.max_h + kBxY - 1) / kBxY, jobs.n);
         k_cost_bt_box<NJ><<<g, 256, smem, st>>>(jobs, maxHalf, nxt);
     }
+    count_launch();
+    // write the int16 volume, read both views' features (and the label base)
+    prof_end(PK_COST, jobs_vox(jobs) * 2 + jobs_px(jobs) * (16 + (J0.refine ? 2 : 0)), st);
     return cudaGetLastError();
 }
 

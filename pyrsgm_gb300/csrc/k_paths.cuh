@@ -36,6 +36,7 @@
 // array directly.
 #pragma once
 
+#include "profiler.h"
 #include "sgm_common.cuh"
 #include "sgm_launch.h"
 
@@ -562,7 +563,11 @@ cudaError_t launch_paths_shape(const Jobs<NJ>& jobs, const LevelExtent& e, cudaS
             if (jobs.d[i].paths >= 3) tbj.d[n++] = jobs.d[i];
         tbj.n = n;
         g.y = n;
+        prof_begin(st);
         k_path_tb<G, K, PYR, NJ><<<g, kTbWarps * 32, smem, st>>>(tbj);
+        count_launch();
+        // read C, write V (int16 per voxel); label base per pixel on refine levels
+        prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * (tbj.d[0].refine ? 2 : 0), st);
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
     }
     constexpr int RPW = 32 / G;
@@ -572,7 +577,19 @@ cudaError_t launch_paths_shape(const Jobs<NJ>& jobs, const LevelExtent& e, cudaS
         if (err != cudaSuccess) return err;
     }
     dim3 g((e.max_h + RPW - 1) / RPW, jobs.n);
+    prof_begin(st);
     k_path_row<G, K, PYR, NJ><<<g, 32, smem, st>>>(jobs);
+    count_launch();
+    if (prof_enabled()) {
+        // read C and the T->B volume, write disparity and confidence (and read the label base)
+        double by = 0;
+        for (int i = 0; i < jobs.n; ++i) {
+            const LevelDesc& d = jobs.d[i];
+            const double px = (double)d.w * d.h;
+            by += px * d.D * (2 + (d.paths >= 3 ? 2 : 0)) + px * (6 + (d.refine ? 2 : 0));
+        }
+        prof_end(PK_PATH_ROW, by, st);
+    }
     return cudaGetLastError();
 }
 

@@ -5,6 +5,7 @@
 // (src/sgm_kernels.cu:1530-1551) and the output copies of
 // pyrsgm_compute_level / pyrsgm_compute_single_scale
 // (src/sgm_kernels.cu:1837-1858, 2053-2069).
+#include "profiler.h"
 #include "sgm_common.cuh"
 #include "sgm_launch.h"
 
@@ -77,7 +78,18 @@ template <int NJ>
 cudaError_t launch_post(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
     dim3 g((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
+    prof_begin(st);
     k_post<NJ><<<g, 256, 0, st>>>(jobs);
+    count_launch();
+    if (prof_enabled()) {
+        double by = 0;
+        for (int i = 0; i < jobs.n; ++i) {
+            const LevelDesc& d = jobs.d[i];
+            const double outb = (d.out16 ? 2 : 0) + (d.out32 ? 4 : 0) + (d.outc ? 4 : 0);
+            by += (double)d.w * d.h * (6 + outb);
+        }
+        prof_end(PK_POST, by, st);
+    }
     return cudaGetLastError();
 }
 

@@ -52,12 +52,31 @@ LevelExtent extent_of(const Jobs<NJ>& j)
     return e;
 }
 
+// Sums over the jobs of a launch (algorithmic-byte accounting).
+template <int NJ>
+double jobs_px(const Jobs<NJ>& j)
+{
+    double s = 0;
+    for (int i = 0; i < j.n; ++i) s += (double)j.d[i].w * j.d[i].h;
+    return s;
+}
+template <int NJ>
+double jobs_vox(const Jobs<NJ>& j)
+{
+    double s = 0;
+    for (int i = 0; i < j.n; ++i) s += (double)j.d[i].w * j.d[i].h * j.d[i].D;
+    return s;
+}
+
 // Aggregation kernel variant: G lanes per path chain, K labels per lane,
 // G*K >= D (padding labels behave as permanently invalid).
 struct PathShape {
     int G, K;
 };
 PathShape path_shape(int D);
+
+// Count of kernel launches issued by this library (process-wide).
+void count_launch();
 
 template <int NB>
 cudaError_t launch_pyrdown(const PyrDownBatch<NB>& b, int max_dw, int max_dh, cudaStream_t st);

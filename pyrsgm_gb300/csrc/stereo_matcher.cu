@@ -100,8 +100,9 @@ Params validateParams(const Params& in)
 }
 
 struct StereoMatcher::Impl {
-    int width = 0, height = 0, levels = 0;
-    Params params;
+    int width = 0, height = 0;
+    Params params;  // declared before `levels`, which is initialised from it
+    int levels = 0;
     std::array<LevelInfo, kMaxLevels + 1> info{};
     void* arena = nullptr;
     size_t arena_bytes = 0;

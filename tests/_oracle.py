@@ -197,6 +197,7 @@ def ref() -> C.CDLL:
         h.ref_last_error.restype = C.c_char_p
         h.ref_create_workspace.restype = _vp
         h.ref_destroy_workspace.argtypes = [_vp]
+        h.ref_workspace_reserve.argtypes = [_vp, _i, _i, _i]
         h.ref_copy_volumes.argtypes = [_vp, _vp, _vp, _vp]
         h.ref_pyrdown_u8.argtypes = [_vp, _sz, _i, _i, _vp, _sz, _i, _i, _vp]
         h.ref_compute_level.argtypes = [_vp] * 8 + [_sz] * 7 + [_i] * 17 + [_f, _i, _f, _f, _f, _f, _vp]
