@@ -33,6 +33,32 @@ int pyrsgm_gb300_workspace_copy_volumes(void* workspace, short* cost, short* agg
 /* Device bytes one workspace of this geometry allocates. */
 size_t pyrsgm_gb300_workspace_bytes(int width, int height, int numDisparities);
 
+/* pyrsgm_compute_level without a workspace, for callers that may not
+ * allocate device memory (hosts that own all device memory, real-time loops
+ * where cudaMalloc's implicit synchronisation is not allowed).  No
+ * counterpart in the reference.  Same arguments (minus the workspace),
+ * results and return codes as pyrsgm_compute_level; the scratch is one
+ * static 32 MiB device array, so a level must fit in it
+ * (pyrsgm_gb300_workspace_bytes(width, height, numDisparities) <= 32 MiB,
+ * e.g. 640x480 at 16 labels) or the call returns -1.  The first call on a
+ * device looks up the array's device address (make it before any stream
+ * capture).  All calls share the array: calls whose GPU work overlaps race
+ * and must be serialised by the caller. */
+int pyrsgm_gb300_compute_level_noalloc(
+    const unsigned char* d_left_gray, const unsigned char* d_right_gray,
+    const short* d_parent_disp, const float* d_parent_conf,
+    short* d_disp, float* d_disp_float, float* d_conf_float,
+    size_t left_step_bytes, size_t right_step_bytes,
+    size_t parent_disp_step_bytes, size_t parent_conf_step_bytes,
+    size_t disp_step_bytes, size_t disp_float_step_bytes, size_t conf_float_step_bytes,
+    int width, int height, int parent_width, int parent_height,
+    int numDisparities, int minDisparity, int maxDisparity,
+    int blockSize, int P1, int P2, int uniquenessRatio, int disp12MaxDiff,
+    int preFilterCap, int costMode, int postFlags, int numPaths, int refineLevel,
+    float minConfidence, int adaptiveP2,
+    float p2Alpha, float p2Beta, float p2LowerMult, float p2UpperMult,
+    cudaStream_t stream);
+
 /* The adaptive-P2 table: d_table[i] (256 ints, device) = the effective P2 for
  * |I(p) - I(p-r)| = i, after the reference's parameter sanitising. */
 int pyrsgm_gb300_p2_table(int* d_table, int P2, float p2Alpha, float p2Beta, float p2LowerMult, float p2UpperMult,

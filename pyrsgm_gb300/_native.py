@@ -42,6 +42,10 @@ _SIGS = {
                                   _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i,
                                   _f, _i, _f, _f, _f, _f, _vp]),
     "pyrsgm_pyrdown_u8": (_i, [_u8p, _sz, _i, _i, _u8p, _sz, _i, _i, _vp]),
+    "pyrsgm_gb300_compute_level_noalloc": (_i, [_u8p, _u8p, _i16p, _f32p, _i16p, _f32p, _f32p,
+                                                _sz, _sz, _sz, _sz, _sz, _sz, _sz,
+                                                _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i,
+                                                _i, _f, _i, _f, _f, _f, _f, _vp]),
     "pyrsgm_gb300_workspace_set_debug": (_i, [_vp, _i]),
     "pyrsgm_gb300_workspace_volumes": (_i, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_i),
                                             C.POINTER(_i), C.POINTER(_i)]),
