@@ -94,6 +94,78 @@ int pyrsgm_gb300_matcher_compute(void* matcher, const unsigned char* d_left, siz
  * and returns the number of levels, or -1 (message in err). */
 int pyrsgm_gb300_level_geometry(int width, int height, const pyrsgm_gb300_params* p, int* out35, char* err,
                                 size_t err_len);
+/* ---- Batched execution (no counterpart in the reference) ----------------
+ * One stereo pair of a batch: device images and outputs as in
+ * StereoMatcher::compute (outputs may be NULL; disp32 without conf uses a
+ * scratch confidence), plus its own size and parameters. */
+typedef struct pyrsgm_gb300_pair {
+    const unsigned char* d_left;
+    size_t left_pitch;
+    const unsigned char* d_right;
+    size_t right_pitch;
+    short* d_disp16;
+    size_t disp16_pitch;
+    float* d_disp32;
+    size_t disp32_pitch;
+    float* d_conf;
+    size_t conf_pitch;
+    int width, height;
+    pyrsgm_gb300_params params;
+} pyrsgm_gb300_pair;
+
+/* A batch engine owns pooled device memory (one arena per pair slot, reused
+ * across runs) up to device_budget_bytes. */
+void* pyrsgm_gb300_batch_create(size_t device_budget_bytes, char* err, size_t err_len);
+void pyrsgm_gb300_batch_destroy(void* engine);
+/* Enqueue all pairs on `stream`: every pyramid stage runs as one launch per
+ * kernel variant for the whole batch.  Results equal StereoMatcher::compute
+ * of each pair alone.  use_graph != 0: the run is captured as a CUDA graph
+ * and replayed by later runs with the same pairs (pointers included); not on
+ * the legacy default stream.  Returns 0, or -1 with the reason in err (bad
+ * parameters, budget exceeded, CUDA error). */
+int pyrsgm_gb300_batch_run(void* engine, const pyrsgm_gb300_pair* pairs, int num_pairs, int use_graph,
+                           cudaStream_t stream, char* err, size_t err_len);
+size_t pyrsgm_gb300_batch_bytes_in_use(void* engine);
+/* Device bytes one pair of this size and parameters occupies in a batch
+ * engine (or a StereoMatcher); 0 for invalid parameters. */
+size_t pyrsgm_gb300_pair_bytes(int width, int height, const pyrsgm_gb300_params* params);
+
+/* ---- Serving: continuous batching (no counterpart in the reference) -------
+ * A request carries HOST images and HOST outputs (pitch = width; outputs may
+ * be NULL).  The caller keeps the buffers alive until the request finished. */
+typedef struct pyrsgm_gb300_request {
+    const unsigned char* h_left;
+    const unsigned char* h_right;
+    short* h_disp16;
+    float* h_disp32;
+    float* h_conf;
+    int width, height;
+    pyrsgm_gb300_params params;
+} pyrsgm_gb300_request;
+
+/* num_streams lanes, each with its own stream, batch engine and
+ * device_budget_bytes / num_streams of pooled device memory; batches of at
+ * most max_batch pairs; at most max_queue requests waiting. */
+void* pyrsgm_gb300_server_create(size_t device_budget_bytes, int max_batch, int num_streams, int max_queue,
+                                 char* err, size_t err_len);
+void pyrsgm_gb300_server_destroy(void* server);
+/* Request id (>= 0), or -1 with the reason in err (invalid request, larger
+ * than a lane's budget, queue full).  Thread-safe. */
+long long pyrsgm_gb300_server_submit(void* server, const pyrsgm_gb300_request* req, char* err, size_t err_len);
+/* 1 = done (outputs written), -1 = failed (reason in err), 0 = timeout
+ * (timeout_s < 0 waits forever).  A finished request's id is released. */
+int pyrsgm_gb300_server_wait(void* server, long long id, double timeout_s, char* err, size_t err_len);
+/* Wait until every submitted request finished: 1, or 0 on timeout. */
+int pyrsgm_gb300_server_drain(void* server, double timeout_s);
+/* out10 = completed, failed, latency p50 / p99 / p99.9 ms (submit -> outputs
+ * in host memory), mean batch size, pairs/s (first submit -> last
+ * completion), peak pairs in flight, refused submissions, max latency ms. */
+int pyrsgm_gb300_server_stats(void* server, double* out10);
+void pyrsgm_gb300_server_reset_stats(void* server);
+/* Test hook: the next `batches` batches fail on the host before reaching the
+ * GPU, as an allocation failure would; their requests report -1. */
+int pyrsgm_gb300_server_inject_failure(void* server, int batches);
+
 /* out[7] = level, width, height, num_labels, max_disparity, block_size, refine */
 int pyrsgm_gb300_matcher_level_info(void* matcher, int level, int* out7);
 int pyrsgm_gb300_matcher_num_levels(void* matcher);

@@ -4,10 +4,10 @@ The product is the native library libpyrsgm_gb300.so (C ABI in
 include/pyrsgm/); this package builds it (pyrsgm_gb300.build) and exposes a
 thin Python surface over it (pyrsgm_gb300.api).
 """
-from .api import (COST_BT, COST_CENSUS, POST_LRCHECK, POST_MEDIAN, LevelInfo, Params, StereoMatcher,
-                  Workspace, compute_level, compute_single_scale, invalid_disparity16, level_geometry,
+from .api import (COST_BT, COST_CENSUS, POST_LRCHECK, POST_MEDIAN, BatchEngine, LevelInfo, Params,
+                  StereoMatcher, Workspace, pair_bytes, compute_level, compute_single_scale, invalid_disparity16, level_geometry,
                   pyrdown, validate_params)
 
-__all__ = ["COST_BT", "COST_CENSUS", "POST_LRCHECK", "POST_MEDIAN", "LevelInfo", "Params", "StereoMatcher",
+__all__ = ["COST_BT", "COST_CENSUS", "POST_LRCHECK", "POST_MEDIAN", "BatchEngine", "LevelInfo", "pair_bytes", "Params", "StereoMatcher",
            "Workspace", "compute_level", "compute_single_scale", "invalid_disparity16", "level_geometry", "pyrdown",
            "validate_params"]

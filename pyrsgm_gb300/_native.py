@@ -29,6 +29,13 @@ class Params(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class Pair(C.Structure):
+    """pyrsgm_gb300_pair: one stereo pair of a batch."""
+    _fields_ = [("d_left", _vp), ("left_pitch", _sz), ("d_right", _vp), ("right_pitch", _sz),
+                ("d_disp16", _vp), ("disp16_pitch", _sz), ("d_disp32", _vp), ("disp32_pitch", _sz),
+                ("d_conf", _vp), ("conf_pitch", _sz), ("width", _i), ("height", _i), ("params", Params)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "pyrsgm_create_workspace": (_vp, []),
@@ -62,6 +69,11 @@ _SIGS = {
     "pyrsgm_gb300_matcher_num_levels": (_i, [_vp]),
     "pyrsgm_gb300_level_geometry": (_i, [_i, _i, C.POINTER(Params), C.POINTER(_i), C.c_char_p, _sz]),
     "pyrsgm_gb300_matcher_device_bytes": (_sz, [_vp]),
+    "pyrsgm_gb300_batch_create": (_vp, [_sz, C.c_char_p, _sz]),
+    "pyrsgm_gb300_batch_destroy": (None, [_vp]),
+    "pyrsgm_gb300_batch_run": (_i, [_vp, C.POINTER(Pair), _i, _i, _vp, C.c_char_p, _sz]),
+    "pyrsgm_gb300_batch_bytes_in_use": (_sz, [_vp]),
+    "pyrsgm_gb300_pair_bytes": (_sz, [_i, _i, C.POINTER(Params)]),
     "pyrsgm_gb300_version": (C.c_char_p, []),
     "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
     "pyrsgm_gb300_profile": (_i, [_i]),

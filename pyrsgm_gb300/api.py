@@ -190,6 +190,58 @@ class StereoMatcher:
         return out
 
 
+def pair_bytes(width: int, height: int, params: Params) -> int:
+    """Device bytes one pair of this shape occupies (StereoMatcher or batch slot)."""
+    return lib().pyrsgm_gb300_pair_bytes(width, height, C.byref(params.to_c()))
+
+
+class BatchEngine:
+    """Many pairs of different shapes per launch (pyrsgm_gb300_batch_*).
+
+    run(items) takes dicts with left, right (uint8 [h, w] device tensors),
+    params (Params) and optional disp16 / disp32 / conf output tensors.
+    """
+
+    def __init__(self, budget_bytes: int):
+        err = C.create_string_buffer(256)
+        self._h = lib().pyrsgm_gb300_batch_create(budget_bytes, err, 256)
+        if not self._h:
+            raise RuntimeError(err.value.decode())
+
+    def bytes_in_use(self) -> int:
+        return lib().pyrsgm_gb300_batch_bytes_in_use(self._h)
+
+    @staticmethod
+    def make_pairs(items: list[dict]):
+        arr = (_native.Pair * len(items))()
+        for i, it in enumerate(items):
+            L, R = it["left"], it["right"]
+            p = arr[i]
+            p.d_left, p.left_pitch = _ptr(L), _pitch(L)
+            p.d_right, p.right_pitch = _ptr(R), _pitch(R)
+            p.d_disp16, p.disp16_pitch = _ptr(it.get("disp16")), _pitch(it.get("disp16"))
+            p.d_disp32, p.disp32_pitch = _ptr(it.get("disp32")), _pitch(it.get("disp32"))
+            p.d_conf, p.conf_pitch = _ptr(it.get("conf")), _pitch(it.get("conf"))
+            p.height, p.width = L.shape
+            p.params = it["params"].to_c()
+        return arr
+
+    def run_pairs(self, arr, use_graph: bool = True, stream=None) -> None:
+        err = C.create_string_buffer(512)
+        if lib().pyrsgm_gb300_batch_run(self._h, arr, len(arr), 1 if use_graph else 0, _stream(stream), err, 512):
+            raise RuntimeError(err.value.decode())
+
+    def run(self, items: list[dict], use_graph: bool = True, stream=None) -> None:
+        self.run_pairs(self.make_pairs(items), use_graph, stream)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().pyrsgm_gb300_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+
 class Workspace:
     """Opaque C-API workspace (pyrsgm_create_workspace / destroy)."""
 

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(256) k_refine_labels(const __grid_constant__ J
     const LevelDesc& J = jobs.d[blockIdx.z];
     const int x = blockIdx.x * 32 + (threadIdx.x & 31);
     const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x >= J.w || y >= J.h) return;
+    if (!J.refine || x >= J.w || y >= J.h) return;
     const int px = imin(x >> 1, J.pw - 1), py = imin(y >> 1, J.ph - 1);
     const int16_t raw = J.pdisp[(size_t)py * J.pd_pitch + px];
     const float conf = J.pconf[(size_t)py * J.pc_pitch + px];

@@ -174,39 +174,98 @@ __device__ __forceinline__ void chain_init(Chain<K>& s, int minD)
 template <int K>
 struct StepIn {
     int c[K];     // matching cost (kMax for an invalid label in pyramid mode)
-    bool lv[K];   // label valid (pyramid)
+    bool lv[K];   // label valid (pyramid); label < D (single-scale)
     int vc;       // number of geometry-valid labels (pyramid)
     int base;     // real disparity of local label 0
     int p2;       // effective P2 towards the previous pixel
 };
 
+// Global inputs of one chain step are loaded pf_depth<K>() steps ahead of
+// their use so that no load latency sits on the serial recurrence (deep for
+// few labels per lane, shallower where the ring would spill registers).
+template <int K>
+__host__ __device__ constexpr int pf_depth()
+{
+    return K <= 2 ? 8 : (K <= 8 ? 4 : 2);
+}
+
+template <int K>
+struct Pre {
+    int c[K];     // cost volume C
+    int v[K];     // aggregation volume V (T->B cost or a first-arrival partial), when needed
+    int base;     // label base (refine levels)
+    int img;      // left intensity (adaptive P2)
+};
+
+template <int K>
+__device__ __forceinline__ void load_k_ro(const int16_t* src, int (&v)[K])
+{
+    if constexpr (K == 1) {
+        v[0] = __ldg(src);
+    } else if constexpr (K == 2) {
+        const uint32_t u = __ldg(reinterpret_cast<const unsigned int*>(src));
+        v[0] = (int16_t)(u & 0xffff);
+        v[1] = (int16_t)(u >> 16);
+    } else if constexpr (K == 4) {
+        const uint2 u = __ldg(reinterpret_cast<const uint2*>(src));
+        v[0] = (int16_t)(u.x & 0xffff); v[1] = (int16_t)(u.x >> 16);
+        v[2] = (int16_t)(u.y & 0xffff); v[3] = (int16_t)(u.y >> 16);
+    } else {
+#pragma unroll
+        for (int i = 0; i < K / 8; ++i) {
+            const uint4 u = __ldg(reinterpret_cast<const uint4*>(src) + i);
+            const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                v[8 * i + 2 * j] = (int16_t)(w[j] & 0xffff);
+                v[8 * i + 2 * j + 1] = (int16_t)(w[j] >> 16);
+            }
+        }
+    }
+}
+
 template <int K, bool PYR>
-__device__ __forceinline__ void load_step(const LevelDesc& J, int y, int x, int gl, StepIn<K>& in)
+__device__ __forceinline__ void prefetch(const LevelDesc& J, int y, int x, int gl, bool need_v, Pre<K>& f)
 {
     const size_t p = (size_t)y * J.w + x;
-    load_labels<K>(J.C + p * J.D, J.D, gl, in.c);
+    const int16_t* cp = J.C + p * J.D;
+    const int d0 = gl * K;
+    if (d0 + K <= J.D) {
+        load_k_ro<K>(cp + d0, f.c);
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; ++k) f.c[k] = (d0 + k < J.D) ? (int)__ldg(cp + d0 + k) : kMax;
+    }
+    if (need_v) load_labels<K>(J.V + p * J.D, J.D, gl, f.v);
+    f.base = (PYR && J.refine) ? (int)__ldg(J.base + p) : J.minD;
+    f.img = J.adaptive ? (int)__ldg(J.left + (size_t)y * J.lstep + x) : 0;
+}
+
+// Label validity of pixel x from its prefetched inputs.
+template <int K, bool PYR>
+__device__ __forceinline__ void make_step(const LevelDesc& J, int x, int gl, const Pre<K>& f, StepIn<K>& in)
+{
+    in.base = f.base;
     if constexpr (PYR) {
-        in.base = J.refine ? (int)J.base[p] : J.minD;
         int lo, hi;
-        label_range(J, x, in.base, lo, hi);
+        label_range(J, x, f.base, lo, hi);
         in.vc = hi >= lo ? hi - lo + 1 : 0;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const int d = gl * K + k;
-            in.lv[k] = d >= lo && d <= hi && in.c[k] < kMax;
-            if (!in.lv[k]) in.c[k] = kMax;
+            in.lv[k] = d >= lo && d <= hi && f.c[k] < kMax;
+            in.c[k] = in.lv[k] ? f.c[k] : kMax;
         }
     } else {
-        in.base = J.minD;
         in.vc = J.D;
 #pragma unroll
-        for (int k = 0; k < K; ++k) in.lv[k] = gl * K + k < J.D;
+        for (int k = 0; k < K; ++k) {
+            in.lv[k] = gl * K + k < J.D;
+            in.c[k] = f.c[k];
+        }
     }
 }
 
-// One step of the path recurrence (src/sgm_kernels.cu:560-565 single-scale,
-// 1230-1252 pyramid).  All lanes of the warp must call it together.
-// xb: this chain's exchange buffer, 2 x (G*K) int16 (K > 1 only).
 template <int G, int K, bool PYR>
 __device__ __forceinline__ void chain_step(Chain<K>& s, const StepIn<K>& in, int P1, int D, int gl,
                                            int16_t* xb, int (&Lc)[K])
@@ -288,91 +347,10 @@ __device__ __forceinline__ unsigned disp2_key(int cost, int x)
     return ((unsigned)cost << 16) | (unsigned)(0xffff - x);
 }
 
-// Winner-take-all of one pixel from the final aggregated costs.
-// Single-scale: src/sgm_kernels.cu:744-808.  Pyramid: 1413-1471.
-template <int G, int K, bool PYR>
-__device__ __forceinline__ void wta(const LevelDesc& J, int y, int x, const int (&tot)[K], const StepIn<K>& in,
-                                    int gl, unsigned* keys, bool active)
-{
-    const int D = J.D;
-    unsigned km = kNoKey;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const int d = gl * K + k;
-        const unsigned key = ((unsigned)(uint16_t)tot[k] << 16) | (unsigned)d;
-        if (d < D && key < km) km = key;
-    }
-    const unsigned best = group_min_u<G>(km);
-    const int minCost = (int)(best >> 16);
-    const int bestD = (int)(best & 0xffffu);
-    int am = kMax;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const int d = gl * K + k;
-        const int dd = d - bestD;
-        if (d < D && (dd > 1 || dd < -1) && (!PYR || in.lv[k])) am = imin(am, tot[k]);
-    }
-    const int alt = group_min<G>(am);
-    int nb[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        const int b = bestD - 1 + j;
-        int v = 0;
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (gl * K + k == b) v = tot[k];
-        nb[j] = __shfl_sync(kFull, v, iclamp(b, 0, D - 1) / K, G);
-    }
-    if (gl != 0 || !active) return;
-    const int16_t inv = (int16_t)((J.minD - 1) * 16);
-    const size_t p = (size_t)y * J.w + x;
-    int16_t dout = inv;
-    float cout = 0.0f;
-    if constexpr (PYR) {
-        bool ok = in.vc >= 3 && minCost < kMax && alt < kMax;
-        if (ok && J.uniq > 0 && alt * (100 - J.uniq) < minCost * 100) ok = false;
-        const int realBest = in.base + bestD;
-        const int physMax = imin(J.maxD, x);
-        if ((bestD == 0 && in.base > J.minD) || (bestD == D - 1 && in.base + D - 1 < physMax)) ok = false;
-        float c = 0.0f;
-        if (ok) {
-            const float den = fmaxf((float)minCost, 1.0f);
-            c = fminf(fmaxf(((float)alt - (float)minCost) / den, 0.0f), 1.0f);
-            if (c < J.minConf) ok = false;
-        }
-        if (ok) {
-            int d16 = realBest * 16;
-            if (bestD > 0 && bestD + 1 < D && nb[0] < kMax && nb[1] < kMax && nb[2] < kMax) {
-                const int den2 = imax(nb[0] + nb[2] - 2 * nb[1], 1);
-                d16 += ((nb[0] - nb[2]) * 16 + den2) / (den2 * 2);
-            }
-            dout = (int16_t)d16;
-            cout = c;
-            const int x2 = x - realBest;
-            if (x2 >= 0 && x2 < J.w) atomicMin(&keys[x2], disp2_key(minCost, x));
-        }
-    } else {
-        bool unique = true;
-        if (J.uniq > 0 && minCost < kMax / 2 && alt * (100 - J.uniq) < minCost * 100) unique = false;
-        if (unique && minCost < kMax / 2) {
-            int dint = bestD * 16;
-            if (bestD > 0 && bestD < D - 1) {
-                const int den2 = imax(nb[0] + nb[2] - 2 * nb[1], 1);
-                dint = bestD * 16 + ((nb[0] - nb[2]) * 16 + den2) / (den2 * 2);
-            }
-            dout = (int16_t)(dint + J.minD * 16);
-            const int x2 = x - bestD - J.minD;
-            if (x2 >= 0 && x2 < J.w) atomicMin(&keys[x2], disp2_key(minCost, x));
-            const float den = fmaxf((float)minCost, 1.0f);
-            cout = fminf(fmaxf(((float)alt - (float)minCost) / den, 0.0f), 1.0f);
-        }
-    }
-    J.disp_raw[p] = dout;
-    J.conf_raw[p] = cout;
-}
-
 // ---------------------------------------------------------------------------
-// Top -> bottom path.  Block: 4 warps; each warp owns 32/G columns.
+// Top -> bottom path.  Block: 4 warps; each warp owns 32/G columns.  The
+// cost, label base and intensity of row y + kPF are loaded while row y is
+// aggregated.
 // ---------------------------------------------------------------------------
 constexpr int kTbWarps = 4;
 
@@ -394,32 +372,144 @@ __global__ void __launch_bounds__(kTbWarps * 32) k_path_tb(const __grid_constant
     if (c0 >= ncols) return;
     const bool active = c0 + grp < ncols;
     const int x = xlo + (active ? c0 + grp : ncols - 1);
+    const int H = J.h;
     int16_t* xb = reinterpret_cast<int16_t*>(sm + 1024) + (warp * CPW + grp) * (2 * G * K);
+    constexpr int kPF = pf_depth<K>();
     Chain<K> s;
     chain_init(s, J.minD);
-    for (int y = 0; y < J.h; ++y) {
-        StepIn<K> in;
-        load_step<K, PYR>(J, y, x, gl, in);
-        in.p2 = J.P2;
-        if (J.adaptive && s.active) {
-            const int a = J.left[(size_t)y * J.lstep + x], b = J.left[(size_t)(y - 1) * J.lstep + x];
-            in.p2 = lut[a > b ? a - b : b - a];
+    Pre<K> ring[kPF];
+#pragma unroll
+    for (int j = 0; j < kPF; ++j)
+        if (j < H) prefetch<K, PYR>(J, j, x, gl, false, ring[j]);
+    int img_prev = 0;
+    for (int y0 = 0; y0 < H; y0 += kPF) {
+#pragma unroll
+        for (int j = 0; j < kPF; ++j) {
+            const int y = y0 + j;
+            if (y < H) {
+                StepIn<K> in;
+                make_step<K, PYR>(J, x, gl, ring[j], in);
+                const int img = ring[j].img;
+                in.p2 = (J.adaptive && s.active) ? lut[abs(img - img_prev) & 255] : J.P2;
+                img_prev = img;
+                if (y + kPF < H) prefetch<K, PYR>(J, y + kPF, x, gl, false, ring[j]);
+                int L[K];
+                chain_step<G, K, PYR>(s, in, J.P1, J.D, gl, xb, L);
+                if (active) store_labels<K>(J.V + ((size_t)y * J.w + x) * J.D, J.D, gl, L);
+            }
         }
-        int L[K];
-        chain_step<G, K, PYR>(s, in, J.P1, J.D, gl, xb, L);
-        if (active) store_labels<K>(J.V + ((size_t)y * J.w + x) * J.D, J.D, gl, L);
     }
 }
 
 // ---------------------------------------------------------------------------
+// Winner-take-all of one pixel from its final aggregated costs, one lane per
+// pixel (deferred: the row kernel stashes each finished pixel's costs and
+// every G steps each lane finishes one of them).
+// Single-scale: src/sgm_kernels.cu:744-808.  Pyramid: 1413-1471.
+// tot: the pixel's D costs (16-byte aligned, D a multiple of 16).
+// ---------------------------------------------------------------------------
+template <bool PYR>
+__device__ __forceinline__ void finish_pixel(const LevelDesc& J, int y, int x, const int16_t* tot, int base, int vc,
+                                             unsigned* keys)
+{
+    const int D = J.D;
+    unsigned best = kNoKey;
+    for (int c = 0; c < D; c += 8) {
+        const uint4 q = *reinterpret_cast<const uint4*>(tot + c);
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const unsigned k0 = ((w[i] & 0xffffu) << 16) | (unsigned)(c + 2 * i);
+            const unsigned k1 = (w[i] & 0xffff0000u) | (unsigned)(c + 2 * i + 1);
+            best = k0 < best ? k0 : best;
+            best = k1 < best ? k1 : best;
+        }
+    }
+    const int minCost = (int)(best >> 16);
+    const int bestD = (int)(best & 0xffffu);
+    int alt = kMax;
+    for (int c = 0; c < D; c += 8) {
+        const uint4 q = *reinterpret_cast<const uint4*>(tot + c);
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int d0 = c + 2 * i;
+            if (d0 < bestD - 1 || d0 > bestD + 1) alt = imin(alt, (int)(int16_t)(w[i] & 0xffff));
+            if (d0 + 1 < bestD - 1 || d0 + 1 > bestD + 1) alt = imin(alt, (int)(int16_t)(w[i] >> 16));
+        }
+    }
+    const int c0 = bestD > 0 ? (int)tot[bestD - 1] : 0;
+    const int c1 = tot[bestD];
+    const int c2 = bestD + 1 < D ? (int)tot[bestD + 1] : 0;
+    const int16_t inv = (int16_t)((J.minD - 1) * 16);
+    int16_t dout = inv;
+    float cout = 0.0f;
+    if constexpr (PYR) {
+        bool ok = vc >= 3 && minCost < kMax && alt < kMax;
+        if (ok && J.uniq > 0 && alt * (100 - J.uniq) < minCost * 100) ok = false;
+        const int realBest = base + bestD;
+        const int physMax = imin(J.maxD, x);
+        if ((bestD == 0 && base > J.minD) || (bestD == D - 1 && base + D - 1 < physMax)) ok = false;
+        float cf = 0.0f;
+        if (ok) {
+            const float den = fmaxf((float)minCost, 1.0f);
+            cf = fminf(fmaxf(((float)alt - (float)minCost) / den, 0.0f), 1.0f);
+            if (cf < J.minConf) ok = false;
+        }
+        if (ok) {
+            int d16 = realBest * 16;
+            if (bestD > 0 && bestD + 1 < D && c0 < kMax && c1 < kMax && c2 < kMax) {
+                const int den2 = imax(c0 + c2 - 2 * c1, 1);
+                d16 += ((c0 - c2) * 16 + den2) / (den2 * 2);
+            }
+            dout = (int16_t)d16;
+            cout = cf;
+            const int x2 = x - realBest;
+            if (x2 >= 0 && x2 < J.w) atomicMin(&keys[x2], disp2_key(minCost, x));
+        }
+    } else {
+        bool unique = true;
+        if (J.uniq > 0 && minCost < kMax / 2 && alt * (100 - J.uniq) < minCost * 100) unique = false;
+        if (unique && minCost < kMax / 2) {
+            int dint = bestD * 16;
+            if (bestD > 0 && bestD < D - 1) {
+                const int den2 = imax(c0 + c2 - 2 * c1, 1);
+                dint = bestD * 16 + ((c0 - c2) * 16 + den2) / (den2 * 2);
+            }
+            dout = (int16_t)(dint + J.minD * 16);
+            const int x2 = x - bestD - J.minD;
+            if (x2 >= 0 && x2 < J.w) atomicMin(&keys[x2], disp2_key(minCost, x));
+            const float den = fmaxf((float)minCost, 1.0f);
+            cout = fminf(fmaxf(((float)alt - (float)minCost) / den, 0.0f), 1.0f);
+        }
+    }
+    const size_t p = (size_t)y * J.w + x;
+    J.disp_raw[p] = dout;
+    J.conf_raw[p] = cout;
+}
+
+// ---------------------------------------------------------------------------
 // Row kernel: L->R and R->L of one row, WTA, disp2, LR check.  One warp per
-// block; each warp owns 32/G rows.
+// block; each warp owns 32/G rows (one per lane group).  Per step both
+// paths advance one pixel; their recurrences are issued back to back
+// (independent dependency chains).  Inputs are prefetched kPF steps ahead.
+// The first path to reach a pixel leaves its partial sum in V, except near
+// the meeting point, where the second path arrives kPF steps later at most:
+// those partials go through a small shared-memory band, so a prefetched V
+// never predates the write it needs.  The path that finishes a pixel stashes
+// the pixel's D total costs in a shared buffer; every G steps each lane
+// finishes one stashed pixel (argmin, second minimum, uniqueness,
+// confidence, sub-pixel, disp2) and the G results are written together.
 // ---------------------------------------------------------------------------
 template <int G, int K, bool PYR, int NJ>
 __global__ void __launch_bounds__(32) k_path_row(const __grid_constant__ Jobs<NJ> jobs)
 {
     const LevelDesc& J = jobs.d[blockIdx.y];
     constexpr int RPW = 32 / G;
+    constexpr int kPF = pf_depth<K>();
+    constexpr int NB = kPF + 2;
+    constexpr int DP = G * K;     // labels including padding
+    constexpr int WS = DP + 8;    // stash row stride (int16): 16-byte rows, spread over banks
     const int W = J.w, H = J.h, D = J.D;
     const int y0 = blockIdx.x * RPW;
     if (y0 >= H) return;
@@ -429,14 +519,19 @@ __global__ void __launch_bounds__(32) k_path_row(const __grid_constant__ Jobs<NJ
 
     extern __shared__ __align__(16) unsigned char sm[];
     int* lut = reinterpret_cast<int*>(sm);
-    unsigned* keys = reinterpret_cast<unsigned*>(sm + 1024) + grp * W;
-    int16_t* xb = reinterpret_cast<int16_t*>(sm + 1024 + (size_t)RPW * W * 4) + grp * (4 * G * K);
+    unsigned char* sp = sm + 1024;
+    int16_t* stash = reinterpret_cast<int16_t*>(sp) + grp * (2 * G * WS);  // [path][slot][WS]
+    sp += (size_t)RPW * 2 * G * WS * 2;
+    int16_t* band = reinterpret_cast<int16_t*>(sp) + grp * (NB * DP);
+    sp += (size_t)RPW * NB * DP * 2;
+    int16_t* xb = reinterpret_cast<int16_t*>(sp) + grp * (4 * DP);
+    sp += (K > 1 ? (size_t)RPW * 4 * DP * 2 : 0);
+    unsigned* keys = reinterpret_cast<unsigned*>(sp) + grp * W;
     if (J.adaptive)
         for (int i = lane; i < 256; i += 32) lut[i] = J.p2lut[i];
     for (int x = gl; x < W; x += G) keys[x] = kNoKey;
     __syncwarp();
 
-    const uint8_t* img = J.left + (size_t)y * J.lstep;
     int minX1 = 0, maxX1 = W, lr_x0 = 0, lr_n, rl_n;
     if (PYR) {
         lr_n = J.paths >= 2 ? W : 0;
@@ -449,80 +544,144 @@ __global__ void __launch_bounds__(32) k_path_row(const __grid_constant__ Jobs<NJ
         rl_n = imax(0, W - minX1);
     }
     const bool has_tb = J.paths >= 3;
+    // a pixel x covered by both paths is reached |2x - C2| steps apart
+    const int C2 = W - 1 + lr_x0;
+    const int band_lo = (C2 - kPF + 1) >> 1;
+    auto in_band = [&](int x) { return abs(2 * x - C2) <= kPF; };
+    auto rl_covers = [&](int x) { return x >= W - rl_n; };
+    auto lr_covers = [&](int x) { return lr_n > 0 && x >= lr_x0 && x < lr_x0 + lr_n; };
+    auto wta_px = [&](int x) { return PYR || (x >= minX1 && x < maxX1 && x != W - 1); };
+    auto pf_lr = [&](int s, Pre<K>& f) {
+        if (s < lr_n) prefetch<K, PYR>(J, y, lr_x0 + s, gl, true, f);
+    };
+    auto pf_rl = [&](int s, Pre<K>& f) {
+        if (s < rl_n) prefetch<K, PYR>(J, y, W - 1 - s, gl, true, f);
+    };
+    // first arrival: fold in T->B, leave the partial in the band or in V
+    auto leave = [&](int x, const int (&L)[K], const int (&vin)[K]) {
+        int part[K];
+        combine_first<K, PYR>(L, vin, has_tb, part);
+        if (in_band(x)) {
+            int16_t* b = band + (x - band_lo) * DP + gl * K;
+#pragma unroll
+            for (int k = 0; k < K; ++k) b[k] = (int16_t)part[k];
+        } else if (active) {
+            store_labels<K>(J.V + ((size_t)y * W + x) * D, D, gl, part);
+        }
+    };
+    // second arrival: the total of all paths
+    auto total = [&](int x, const int (&L)[K], const int (&vin)[K], int (&tot)[K]) {
+        int part[K];
+        if (in_band(x)) {
+            const int16_t* b = band + (x - band_lo) * DP + gl * K;
+#pragma unroll
+            for (int k = 0; k < K; ++k) part[k] = b[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; ++k) part[k] = vin[k];
+        }
+        combine_second<K, PYR>(part, L, tot);
+        if (J.debug_acc && active) store_labels<K>(J.V + ((size_t)y * W + x) * D, D, gl, tot);
+    };
+    // deferred WTA: slot `slot` of path `path` holds pixel wx[path] of lane `slot`
+    int wx[2] = {-1, -1}, wbase[2] = {0, 0}, wvc[2] = {0, 0};
+    auto stash_px = [&](int path, int slot, int x, const int (&tot)[K], const StepIn<K>& in) {
+        int16_t* s = stash + (path * G + slot) * WS + gl * K;
+#pragma unroll
+        for (int k = 0; k < K; ++k) s[k] = (int16_t)tot[k];
+        if (gl == slot) {
+            wx[path] = x;
+            wbase[path] = in.base;
+            wvc[path] = in.vc;
+        }
+    };
+    auto flush = [&]() {
+        __syncwarp();
+#pragma unroll
+        for (int path = 0; path < 2; ++path) {
+            if (wx[path] >= 0 && active)
+                finish_pixel<PYR>(J, y, wx[path], stash + (path * G + gl) * WS, wbase[path], wvc[path], keys);
+            wx[path] = -1;
+        }
+        __syncwarp();
+    };
+
     Chain<K> lr, rl;
     chain_init(lr, J.minD);
     chain_init(rl, J.minD);
+    // Value-initialised: without an L->R path (numPaths == 1) its ring is never
+    // loaded, yet its recurrence still runs (idle) beside the R->L one.
+    Pre<K> plr[kPF] = {}, prl[kPF] = {};
+#pragma unroll
+    for (int j = 0; j < kPF; ++j) {
+        pf_lr(j, plr[j]);
+        pf_rl(j, prl[j]);
+    }
+    int lr_img_prev = 0, rl_img_prev = 0;
+    const bool has_lr = lr_n > 0;
     const int T = imax(lr_n, rl_n);
-    for (int t = 0; t < T; ++t) {
-        if (t < lr_n) {
-            const int x = lr_x0 + t;
-            StepIn<K> in;
-            load_step<K, PYR>(J, y, x, gl, in);
-            in.p2 = J.P2;
-            if (J.adaptive && lr.active) {
-                const int a = img[x], b = img[x - 1];
-                in.p2 = lut[a > b ? a - b : b - a];
-            }
-            int L[K];
-            chain_step<G, K, PYR>(lr, in, J.P1, D, gl, xb, L);
-            int16_t* vp = J.V + ((size_t)y * W + x) * D;
-            const bool rl_cov = x >= W - rl_n;
-            if (rl_cov && (W - 1 - x) < t) {
-                int part[K], tot[K];
-                load_labels<K>(vp, D, gl, part);
-                combine_second<K, PYR>(part, L, tot);
-                if (J.debug_acc && active) store_labels<K>(vp, D, gl, tot);
-                if (PYR || x != W - 1) wta<G, K, PYR>(J, y, x, tot, in, gl, keys, active);
-            } else if (rl_cov) {
-                int tb[K], part[K];
-                if (has_tb) load_labels<K>(vp, D, gl, tb);
-                combine_first<K, PYR>(L, tb, has_tb, part);
-                if (active) store_labels<K>(vp, D, gl, part);
-            }
-        }
-        if (t < rl_n) {
-            const int x = W - 1 - t;
-            StepIn<K> in;
-            load_step<K, PYR>(J, y, x, gl, in);
-            in.p2 = J.P2;
-            if (J.adaptive && rl.active) {
-                const int a = img[x], b = img[x + 1];
-                in.p2 = lut[a > b ? a - b : b - a];
-            }
-            int L[K];
-            chain_step<G, K, PYR>(rl, in, J.P1, D, gl, xb + 2 * G * K, L);
-            int16_t* vp = J.V + ((size_t)y * W + x) * D;
-            const bool wta_px = PYR || (x >= minX1 && x < maxX1 && x != W - 1);
-            const bool lr_cov = lr_n > 0 && x >= lr_x0 && x < lr_x0 + lr_n;
-            if (lr_n == 0) {
-                // R->L is the only horizontal path (and there is no T->B)
-                if (J.debug_acc && active) store_labels<K>(vp, D, gl, L);
-                if (wta_px) wta<G, K, PYR>(J, y, x, L, in, gl, keys, active);
-            } else if (lr_cov && (x - lr_x0) <= t) {
-                int part[K], tot[K];
-                load_labels<K>(vp, D, gl, part);
-                combine_second<K, PYR>(part, L, tot);
-                if (J.debug_acc && active) store_labels<K>(vp, D, gl, tot);
-                if (wta_px) wta<G, K, PYR>(J, y, x, tot, in, gl, keys, active);
-            } else if (lr_cov) {
-                int tb[K], part[K];
-                if (has_tb) load_labels<K>(vp, D, gl, tb);
-                combine_first<K, PYR>(L, tb, has_tb, part);
-                if (active) store_labels<K>(vp, D, gl, part);
+    for (int t0 = 0; t0 < T; t0 += kPF) {
+#pragma unroll
+        for (int j = 0; j < kPF; ++j) {
+            const int t = t0 + j;
+            if (t < T) {
+                const int xl = lr_x0 + imin(t, imax(lr_n - 1, 0));
+                const int xr = W - 1 - imin(t, rl_n - 1);
+                StepIn<K> il, ir;
+                make_step<K, PYR>(J, xl, gl, plr[j], il);
+                make_step<K, PYR>(J, xr, gl, prl[j], ir);
+                il.p2 = (J.adaptive && lr.active) ? lut[abs(plr[j].img - lr_img_prev) & 255] : J.P2;
+                ir.p2 = (J.adaptive && rl.active) ? lut[abs(prl[j].img - rl_img_prev) & 255] : J.P2;
+                lr_img_prev = plr[j].img;
+                rl_img_prev = prl[j].img;
+                int vl[K], vr[K];
+#pragma unroll
+                for (int k = 0; k < K; ++k) { vl[k] = plr[j].v[k]; vr[k] = prl[j].v[k]; }
+                pf_lr(t + kPF, plr[j]);
+                pf_rl(t + kPF, prl[j]);
+                // both recurrences back to back (a finished L->R path only idles)
+                int Ll[K], Lr[K];
+                chain_step<G, K, PYR>(lr, il, J.P1, D, gl, xb, Ll);
+                chain_step<G, K, PYR>(rl, ir, J.P1, D, gl, xb + 2 * DP, Lr);
+                const int slot = t & (G - 1);
+                if (has_lr && t < lr_n && rl_covers(xl)) {
+                    if ((W - 1 - xl) < t) {
+                        int tot[K];
+                        total(xl, Ll, vl, tot);
+                        if (wta_px(xl)) stash_px(0, slot, xl, tot, il);
+                    } else {
+                        leave(xl, Ll, vl);
+                    }
+                }
+                if (t < rl_n) {
+                    if (!has_lr) {
+                        // R->L is the only horizontal path (and there is no T->B)
+                        if (J.debug_acc && active) store_labels<K>(J.V + ((size_t)y * W + xr) * D, D, gl, Lr);
+                        if (wta_px(xr)) stash_px(1, slot, xr, Lr, ir);
+                    } else if (lr_covers(xr)) {
+                        if ((xr - lr_x0) <= t) {
+                            int tot[K];
+                            total(xr, Lr, vr, tot);
+                            if (wta_px(xr)) stash_px(1, slot, xr, tot, ir);
+                        } else {
+                            leave(xr, Lr, vr);
+                        }
+                    }
+                }
+                if (slot == G - 1 || t == T - 1) flush();
             }
         }
     }
-    __syncwarp();
 
     // LR check over the finished row and the final per-pixel write.
     const int16_t inv = (int16_t)((J.minD - 1) * 16);
     const bool check = (J.post & POST_LRCHECK) != 0;
     for (int x = gl; x < W; x += G) {
-        const size_t p = (size_t)y * W + x;
-        const bool wp = PYR || (x >= minX1 && x < maxX1 && x != W - 1);
+        const size_t pp = (size_t)y * W + x;
+        const bool wp = wta_px(x);
         int d16 = inv;
         float cf = 0.0f;
-        if (wp) { d16 = J.disp_raw[p]; cf = J.conf_raw[p]; }
+        if (wp) { d16 = J.disp_raw[pp]; cf = J.conf_raw[pp]; }
         if (check && d16 != inv) {
             const int d0 = d16 >> 4, d1 = (d16 + 15) >> 4;
             const int r0 = x - d0, r1 = x - d1;
@@ -542,7 +701,7 @@ __global__ void __launch_bounds__(32) k_path_row(const __grid_constant__ Jobs<NJ
                 if (bad0 && bad1) { d16 = inv; cf = 0.0f; }
             }
         }
-        if (active) { J.disp_raw[p] = (int16_t)d16; J.conf_raw[p] = cf; }
+        if (active) { J.disp_raw[pp] = (int16_t)d16; J.conf_raw[pp] = cf; }
     }
 }
 
@@ -571,7 +730,9 @@ cudaError_t launch_paths_shape(const Jobs<NJ>& jobs, const LevelExtent& e, cudaS
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
     }
     constexpr int RPW = 32 / G;
-    const size_t smem = 1024 + (size_t)RPW * e.max_w * 4 + (K > 1 ? (size_t)RPW * 4 * G * K * 2 : 0);
+    constexpr int DP = G * K;
+    const size_t smem = 1024 + (size_t)RPW * 2 * G * (DP + 8) * 2 + (size_t)RPW * (pf_depth<K>() + 2) * DP * 2 +
+                        (K > 1 ? (size_t)RPW * 4 * DP * 2 : 0) + (size_t)RPW * e.max_w * 4;
     if (smem > 48 * 1024) {
         err = cudaFuncSetAttribute(k_path_row<G, K, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return err;

@@ -75,8 +75,11 @@ struct PathShape {
 };
 PathShape path_shape(int D);
 
-// Count of kernel launches issued by this library (process-wide).
+// Count of kernel launches issued by this library (process-wide); a CUDA
+// graph replay counts the kernels it contains.
 void count_launch();
+void count_launches(unsigned long long n);
+unsigned long long launch_count();
 
 template <int NB>
 cudaError_t launch_pyrdown(const PyrDownBatch<NB>& b, int max_dw, int max_dh, cudaStream_t st);

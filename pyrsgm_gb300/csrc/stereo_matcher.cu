@@ -19,6 +19,7 @@
 #include "pyrsgm/pyrsgm.h"
 #include "pyrsgm/pyrsgm_c.h"
 #include "pyrsgm/pyrsgm_gb300.h"
+#include "pair_plan.h"
 #include "sgm_launch.h"
 #include "workspace.h"
 
@@ -36,12 +37,10 @@ int align16(int v) { return std::max(16, ((v + 15) / 16) * 16); }
     throw std::runtime_error("pyrsgm: " + what + ": " + cudaGetErrorString(err));
 }
 
-size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
-
 }  // namespace
 
 // Level geometry of a validated parameter set, src/stereo_matcher.cpp:169-193.
-void levelGeometry(int w, int h, const Params& params, std::array<LevelInfo, kMaxLevels + 1>& info)
+void levelGeometry(int w, int h, const Params& params, std::array<LevelInfo, 5>& info)
 {
     const int levels = params.pyramid_levels;
     int lw = w, lh = h;
@@ -100,143 +99,19 @@ Params validateParams(const Params& in)
 }
 
 struct StereoMatcher::Impl {
-    int width = 0, height = 0;
-    Params params;  // declared before `levels`, which is initialised from it
-    int levels = 0;
-    std::array<LevelInfo, kMaxLevels + 1> info{};
-    void* arena = nullptr;
-    size_t arena_bytes = 0;
-    std::array<pg::Workspace, kMaxLevels + 1> ws{};
-    std::array<uint8_t*, kMaxLevels + 1> pyrL{}, pyrR{};
-    std::array<int16_t*, kMaxLevels + 1> disp16{};
-    std::array<float*, kMaxLevels + 1> conf{};
-    std::array<int, kMaxLevels + 1> pitch8{}, pitch16{}, pitch32{};  // bytes / elements / elements
-    float* conf0 = nullptr;
-    int* lut = nullptr;
-    float alpha = 0, beta = 0, lower = 0, upper = 0;
-    int adaptive = 0;
+    pg::PairPlan plan;
 
-    Impl(int w, int h, const Params& p) : width(w), height(h), params(validateParams(p)), levels(params.pyramid_levels)
+    Impl(int w, int h, const Params& p) : plan(checkedSize(w, h), h, validateParams(p))
+    {
+        // the P2 table was enqueued on the legacy default stream; compute() may use any stream
+        const cudaError_t err = cudaDeviceSynchronize();
+        if (err != cudaSuccess) throwCuda("adaptive P2 table", err);
+    }
+
+    static int checkedSize(int w, int h)
     {
         if (w <= 0 || h <= 0) throw std::invalid_argument("pyrsgm: empty image size");
-        levelGeometry(w, h, params, info);
-        // one arena: workspaces, pyramid images, intermediate outputs, scratch conf, P2 table
-        size_t total = 0;
-        std::array<size_t, kMaxLevels + 1> ws_off{}, img_off{}, out_off{};
-        for (int level = 0; level <= levels; ++level) {
-            const LevelInfo& li = info[level];
-            ws_off[level] = total;
-            total += al256(pg::Workspace::bytes_for(li.width, li.height, li.num_labels));
-            if (level > 0) {
-                pitch8[level] = (int)al256(li.width);
-                pitch16[level] = (int)(al256((size_t)li.width * 2) / 2);
-                pitch32[level] = (int)(al256((size_t)li.width * 4) / 4);
-                img_off[level] = total;
-                total += al256((size_t)pitch8[level] * li.height) * 2;
-                out_off[level] = total;
-                total += al256((size_t)pitch16[level] * 2 * li.height) + al256((size_t)pitch32[level] * 4 * li.height);
-            }
-        }
-        const size_t conf0_off = total;
-        total += al256((size_t)w * h * 4);
-        const size_t lut_off = total;
-        total += 1024;
-        cudaError_t err = cudaMalloc(&arena, total);
-        if (err != cudaSuccess) { arena = nullptr; throwCuda("arena allocation", err); }
-        arena_bytes = total;
-        auto* base = static_cast<unsigned char*>(arena);
-        for (int level = 0; level <= levels; ++level) {
-            const LevelInfo& li = info[level];
-            ws[level].carve(base + ws_off[level], li.width, li.height, li.num_labels);
-            ws[level].owned = false;
-            ws[level].mem = base + ws_off[level];
-            if (level > 0) {
-                pyrL[level] = base + img_off[level];
-                pyrR[level] = pyrL[level] + al256((size_t)pitch8[level] * li.height);
-                disp16[level] = reinterpret_cast<int16_t*>(base + out_off[level]);
-                conf[level] = reinterpret_cast<float*>(base + out_off[level] +
-                                                       al256((size_t)pitch16[level] * 2 * li.height));
-            }
-        }
-        conf0 = reinterpret_cast<float*>(base + conf0_off);
-        lut = reinterpret_cast<int*>(base + lut_off);
-        adaptive = params.adaptive_p2 ? 1 : 0;
-        alpha = params.p2_alpha; beta = params.p2_beta; lower = params.p2_lower_mult; upper = params.p2_upper_mult;
-        pg::sanitize_p2(adaptive, alpha, beta, lower, upper);
-        if (adaptive) {
-            err = pg::launch_p2_table(lut, params.p2, alpha, beta, lower, upper, nullptr);
-            if (err == cudaSuccess) err = cudaDeviceSynchronize();
-            if (err != cudaSuccess) { release(); throwCuda("adaptive P2 table", err); }
-        }
-    }
-
-    ~Impl() { release(); }
-
-    void release()
-    {
-        if (arena) cudaFree(arena);
-        arena = nullptr;
-    }
-
-    int postFlags(int level) const
-    {
-        // src/stereo_matcher.cpp:229-236
-        if (level != 0) return PYRSGM_POST_LRCHECK;
-        return (params.lr_check ? PYRSGM_POST_LRCHECK : 0) | (params.median_filter ? PYRSGM_POST_MEDIAN : 0);
-    }
-
-    pg::LevelDesc levelDesc(int level) const
-    {
-        const LevelInfo& li = info[level];
-        pg::LevelDesc d;
-        std::memset(&d, 0, sizeof d);
-        d.w = li.width;
-        d.h = li.height;
-        d.D = li.num_labels;
-        d.minD = params.min_disparity;
-        d.pyr = levels > 0 ? 1 : 0;
-        d.refine = li.refine ? 1 : 0;
-        d.cost = params.cost_mode == CostMode::Census ? pg::COST_CENSUS : pg::COST_BT;
-        d.bs = li.block_size;
-        d.pfc = params.pre_filter_cap;
-        d.P1 = params.p1;
-        d.P2 = params.p2;
-        d.uniq = params.uniqueness_ratio;
-        d.maxdiff = params.disp12_max_diff;
-        d.post = postFlags(level);
-        d.paths = params.num_paths;
-        d.adaptive = adaptive;
-        d.minConf = params.pyramid_min_confidence;
-        d.conf_only_copy = d.pyr;
-        if (d.pyr) {
-            // pyrsgm_compute_level clamps, src/sgm_kernels.cu:1661-1665
-            int maxD = std::min(li.max_disparity, li.width - 1);
-            maxD = std::min(maxD, SHRT_MAX / 16);
-            if (!li.refine) maxD = std::min(maxD, d.minD + d.D - 1);
-            d.maxD = maxD;
-        } else {
-            d.maxD = d.minD + d.D - 1;
-        }
-        pg::fill_workspace_ptrs(d, ws[level]);
-        d.p2lut = lut;
-        if (level > 0) {
-            d.left = pyrL[level];
-            d.right = pyrR[level];
-            d.lstep = d.rstep = pitch8[level];
-            d.out16 = disp16[level];
-            d.out16_pitch = pitch16[level];
-            d.outc = conf[level];
-            d.outc_pitch = pitch32[level];
-        }
-        if (li.refine) {
-            d.pdisp = disp16[level + 1];
-            d.pconf = conf[level + 1];
-            d.pd_pitch = pitch16[level + 1];
-            d.pc_pitch = pitch32[level + 1];
-            d.pw = info[level + 1].width;
-            d.ph = info[level + 1].height;
-        }
-        return d;
+        return w;
     }
 
     void runLevel(const pg::LevelDesc& d, int level, cudaStream_t st)
@@ -250,7 +125,7 @@ struct StereoMatcher::Impl {
         if (err == cudaSuccess) err = pg::launch_paths(j, e, st);
         if (err == cudaSuccess) err = pg::launch_post(j, e, st);
         if (err != cudaSuccess) {
-            const LevelInfo& li = info[level];
+            const LevelInfo& li = plan.info[level];
             std::ostringstream oss;
             oss << "pyramid level " << level << " (" << li.width << "x" << li.height << ", D=" << li.num_labels
                 << ", refine=" << li.refine << ")";
@@ -264,40 +139,17 @@ struct StereoMatcher::Impl {
         if (!L || !R) throw std::invalid_argument("pyrsgm: null input image");
         if (!d16 && !d32 && !c) return;
         if (d16 && (d16p % 2) != 0) throw std::invalid_argument("pyrsgm: disp16 pitch must be even");
-        float* oc = c;
-        size_t ocp = cp;
-        if (!oc && d32) { oc = conf0; ocp = (size_t)width * 4; }
-        if (levels > 0) {
-            // both views of a level in one launch
-            for (int level = 1; level <= levels; ++level) {
-                const LevelInfo& par = info[level - 1];
-                const LevelInfo& li = info[level];
-                pg::PyrDownBatch<2> b;
-                b.n = 2;
-                const uint8_t* sl = level == 1 ? L : pyrL[level - 1];
-                const uint8_t* sr = level == 1 ? R : pyrR[level - 1];
-                const int sls = level == 1 ? (int)lp : pitch8[level - 1];
-                const int srs = level == 1 ? (int)rp : pitch8[level - 1];
-                b.d[0] = {sl, pyrL[level], sls, par.width, par.height, pitch8[level], li.width, li.height};
-                b.d[1] = {sr, pyrR[level], srs, par.width, par.height, pitch8[level], li.width, li.height};
-                cudaError_t err = pg::launch_pyrdown(b, li.width, li.height, st);
-                if (err != cudaSuccess) throwCuda("pyrDown", err);
-            }
+        // both views of a pyramid level in one launch
+        for (int level = 1; level <= plan.levels; ++level) {
+            pg::PyrDownBatch<2> b;
+            b.n = 2;
+            plan.pyrdownDescs(level, L, lp, R, rp, b.d);
+            const cudaError_t err = pg::launch_pyrdown(b, plan.info[level].width, plan.info[level].height, st);
+            if (err != cudaSuccess) throwCuda("pyrDown", err);
         }
-        for (int level = levels; level >= 0; --level) {
-            pg::LevelDesc d = levelDesc(level);
-            if (level == 0) {
-                d.left = L;
-                d.right = R;
-                d.lstep = (int)lp;
-                d.rstep = (int)rp;
-                d.out16 = d16;
-                d.out16_pitch = (int)(d16p / 2);
-                d.out32 = d32;
-                d.out32_pitch = (int)(d32p / 4);
-                d.outc = oc;
-                d.outc_pitch = (int)(ocp / 4);
-            }
+        for (int level = plan.levels; level >= 0; --level) {
+            const pg::LevelDesc d =
+                level == 0 ? plan.level0(L, lp, R, rp, d16, d16p, d32, d32p, c, cp) : plan.levelDesc(level);
             runLevel(d, level, st);
         }
     }
@@ -316,16 +168,16 @@ void StereoMatcher::compute(const uint8_t* d_left, size_t left_pitch, const uint
                    conf_pitch, stream);
 }
 
-int StereoMatcher::width() const { return impl_->width; }
-int StereoMatcher::height() const { return impl_->height; }
-const Params& StereoMatcher::params() const { return impl_->params; }
-int StereoMatcher::numLevels() const { return impl_->levels + 1; }
+int StereoMatcher::width() const { return impl_->plan.width; }
+int StereoMatcher::height() const { return impl_->plan.height; }
+const Params& StereoMatcher::params() const { return impl_->plan.params; }
+int StereoMatcher::numLevels() const { return impl_->plan.levels + 1; }
 LevelInfo StereoMatcher::levelInfo(int level) const
 {
-    if (level < 0 || level > impl_->levels) throw std::out_of_range("pyrsgm: level");
-    return impl_->info[level];
+    if (level < 0 || level > impl_->plan.levels) throw std::out_of_range("pyrsgm: level");
+    return impl_->plan.info[level];
 }
-size_t StereoMatcher::deviceMemoryBytes() const { return impl_->arena_bytes; }
+size_t StereoMatcher::deviceMemoryBytes() const { return impl_->plan.arena_bytes; }
 
 const char* version() { return "0.1.0"; }
 
