@@ -1,0 +1,531 @@
+// server.cu -- continuous-batching stereo server.  No counterpart in the
+// reference (one pair per blocking-free call, no request handling).
+//
+// Requests carry host images and host output buffers.  A scheduler thread
+// forms a batch from whatever has arrived as soon as one of the server's
+// stream lanes is free (up to max_batch pairs and the lane's device budget),
+// copies the inputs through pinned staging, runs the lane's batch engine and
+// copies the outputs back, all asynchronously on the lane's stream; while
+// one lane's batch is on the GPU the next lane takes the requests that
+// arrived meanwhile, so batches overlap on the device.  A completion thread
+// waits for each lane's event in order, hands the results to the callers'
+// buffers and records the latency (submit -> results in host memory).
+//
+// Device memory stays resident: each lane keeps its batch engine's pooled
+// pair plans and a pool of input/output buffers per image size.  A request
+// is admitted only if it fits a lane's budget on its own; a batch is cut
+// where the next request would push the lane past its budget.  Failures are
+// per request (status -1 with a message): an invalid request is refused at
+// submission, a full queue refuses new requests, and a batch whose
+// allocation or launch fails fails its own requests while the server keeps
+// serving.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "pair_plan.h"
+#include "pyrsgm/pyrsgm_gb300.h"
+
+namespace pyrsgm {
+Params validateParams(const Params& in);
+}
+
+namespace pg {
+
+double now_s()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+    long long id = 0;
+    pyrsgm_gb300_request r{};
+    size_t bytes = 0;
+    double t_submit = 0, t_done = 0;
+    int status = 0;  // 0 pending, 1 done, -1 failed
+    std::string error;
+};
+
+// Device and pinned-host I/O buffers of one image size.
+struct IOBuf {
+    int w = 0, h = 0;
+    unsigned char *dL = nullptr, *dR = nullptr, *hL = nullptr, *hR = nullptr;
+    short* d16 = nullptr;
+    float *d32 = nullptr, *dc = nullptr;
+    short* h16 = nullptr;
+    float *h32 = nullptr, *hc = nullptr;
+    size_t device_bytes() const { return (size_t)w * h * (2 + 2 + 4 + 4); }
+    void alloc(int W_, int H_)
+    {
+        w = W_;
+        h = H_;
+        const size_t px = (size_t)w * h;
+        auto ok = [](cudaError_t e) {
+            if (e != cudaSuccess) throw std::runtime_error(std::string("server buffers: ") + cudaGetErrorString(e));
+        };
+        ok(cudaMalloc(&dL, px));
+        ok(cudaMalloc(&dR, px));
+        ok(cudaMalloc(&d16, px * 2));
+        ok(cudaMalloc(&d32, px * 4));
+        ok(cudaMalloc(&dc, px * 4));
+        ok(cudaHostAlloc(&hL, px, cudaHostAllocDefault));
+        ok(cudaHostAlloc(&hR, px, cudaHostAllocDefault));
+        ok(cudaHostAlloc(&h16, px * 2, cudaHostAllocDefault));
+        ok(cudaHostAlloc(&h32, px * 4, cudaHostAllocDefault));
+        ok(cudaHostAlloc(&hc, px * 4, cudaHostAllocDefault));
+    }
+    void release()
+    {
+        for (void* p : {(void*)dL, (void*)dR, (void*)d16, (void*)d32, (void*)dc})
+            if (p) cudaFree(p);
+        for (void* p : {(void*)hL, (void*)hR, (void*)h16, (void*)h32, (void*)hc})
+            if (p) cudaFreeHost(p);
+        dL = dR = hL = hR = nullptr;
+        d16 = h16 = nullptr;
+        d32 = dc = h32 = hc = nullptr;
+    }
+};
+
+class BatchEngine;
+BatchEngine* batch_engine_new(size_t budget);
+void batch_engine_delete(BatchEngine* e);
+void batch_engine_run(BatchEngine* e, const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph);
+
+struct Lane {
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
+    BatchEngine* eng = nullptr;
+    std::map<std::pair<int, int>, std::vector<std::unique_ptr<IOBuf>>> pool;
+    std::vector<Request*> reqs;
+    std::vector<IOBuf*> bufs;
+    bool busy = false;
+    std::string error;  // set when the batch failed before reaching the GPU
+};
+
+class Server {
+public:
+    Server(size_t budget, int max_batch, int lanes, int max_queue)
+        : max_batch_(std::max(1, max_batch)), max_queue_(std::max(1, max_queue))
+    {
+        const int n = std::max(1, lanes);
+        lane_budget_ = budget / n;
+        for (int i = 0; i < n; ++i) {
+            auto L = std::make_unique<Lane>();
+            if (cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming) != cudaSuccess)
+                throw std::runtime_error("server: stream/event creation failed");
+            L->eng = batch_engine_new(lane_budget_);
+            lanes_.push_back(std::move(L));
+        }
+        sched_ = std::thread([this] { schedule(); });
+        comp_ = std::thread([this] { complete(); });
+    }
+
+    ~Server()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        sched_.join();
+        comp_.join();
+        for (auto& L : lanes_) {
+            cudaStreamSynchronize(L->st);
+            for (auto& kv : L->pool)
+                for (auto& b : kv.second) b->release();
+            batch_engine_delete(L->eng);
+            cudaEventDestroy(L->done);
+            cudaStreamDestroy(L->st);
+        }
+    }
+
+    long long submit(const pyrsgm_gb300_request& r, std::string& err)
+    {
+        if (r.width <= 0 || r.height <= 0 || !r.h_left || !r.h_right) {
+            err = "invalid request: empty size or null image";
+            return -1;
+        }
+        pyrsgm::Params v;
+        try {
+            v = pyrsgm::validateParams(toParams(r.params));
+        } catch (const std::exception& e) {
+            err = std::string("invalid request: ") + e.what();
+            return -1;
+        }
+        auto q = std::make_unique<Request>();
+        q->r = r;
+        q->bytes = PairPlan::bytesFor(r.width, r.height, v) + (size_t)r.width * r.height * 12;
+        if (q->bytes > lane_budget_) {
+            err = "request needs " + std::to_string(q->bytes) + " device bytes, more than a lane's budget (" +
+                  std::to_string(lane_budget_) + ")";
+            return -1;
+        }
+        std::lock_guard<std::mutex> lk(mu_);
+        if ((int)queue_.size() >= max_queue_) {
+            err = "queue full";
+            ++refused_;
+            return -1;
+        }
+        q->id = next_id_++;
+        q->t_submit = now_s();
+        if (first_submit_ == 0) first_submit_ = q->t_submit;
+        Request* raw = q.get();
+        all_[raw->id] = std::move(q);
+        queue_.push_back(raw);
+        cv_.notify_all();
+        return raw->id;
+    }
+
+    // 1 done, -1 failed (err set), 0 timed out.  A finished request is forgotten.
+    int wait(long long id, double timeout_s, std::string& err)
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        auto it = all_.find(id);
+        if (it == all_.end()) {
+            err = "unknown request id";
+            return -1;
+        }
+        Request* q = it->second.get();
+        const auto pred = [&] { return q->status != 0; };
+        if (timeout_s < 0) done_cv_.wait(lk, pred);
+        else if (!done_cv_.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return 0;
+        const int s = q->status;
+        err = q->error;
+        all_.erase(it);
+        return s;
+    }
+
+    // Wait until every submitted request finished; 1, or 0 on timeout.
+    int drain(double timeout_s)
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        const auto pred = [&] { return queue_.empty() && inflight_ == 0; };
+        if (timeout_s < 0) {
+            done_cv_.wait(lk, pred);
+            return 1;
+        }
+        return done_cv_.wait_for(lk, std::chrono::duration<double>(timeout_s), pred) ? 1 : 0;
+    }
+
+    void stats(double* o)
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        std::vector<double> l = lat_ms_;
+        std::sort(l.begin(), l.end());
+        auto pct = [&](double q) { return l.empty() ? 0.0 : l[std::min(l.size() - 1, (size_t)(q * (l.size() - 1) + 0.5))]; };
+        o[0] = (double)ok_;
+        o[1] = (double)failed_;
+        o[2] = pct(0.50);
+        o[3] = pct(0.99);
+        o[4] = pct(0.999);
+        o[5] = batches_ ? (double)batched_pairs_ / batches_ : 0.0;
+        o[6] = (last_done_ > first_submit_ && ok_) ? ok_ / (last_done_ - first_submit_) : 0.0;
+        o[7] = (double)max_inflight_pairs_;
+        o[8] = (double)refused_;
+        o[9] = l.empty() ? 0.0 : l.back();
+    }
+
+    void reset_stats()
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        lat_ms_.clear();
+        ok_ = failed_ = refused_ = 0;
+        batches_ = batched_pairs_ = 0;
+        max_inflight_pairs_ = 0;
+        first_submit_ = last_done_ = 0;
+    }
+
+    void inject_failure(int n)
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        inject_ += n;
+    }
+
+private:
+    static pyrsgm::Params toParams(const pyrsgm_gb300_params& c)
+    {
+        pyrsgm::Params p;
+        p.num_disparities = c.num_disparities;
+        p.min_disparity = c.min_disparity;
+        p.block_size = c.block_size;
+        p.cost_mode = c.cost_mode == 1 ? pyrsgm::CostMode::Census : pyrsgm::CostMode::BirchfieldTomasi;
+        p.p1 = c.p1;
+        p.p2 = c.p2;
+        p.uniqueness_ratio = c.uniqueness_ratio;
+        p.disp12_max_diff = c.disp12_max_diff;
+        p.lr_check = c.lr_check != 0;
+        p.median_filter = c.median_filter != 0;
+        p.num_paths = c.num_paths;
+        p.pre_filter_cap = c.pre_filter_cap;
+        p.pyramid_levels = c.pyramid_levels;
+        p.pyramid_coarse_disparities = c.pyramid_coarse_disparities;
+        p.pyramid_max_disparity = c.pyramid_max_disparity;
+        p.pyramid_min_confidence = c.pyramid_min_confidence;
+        p.adaptive_p2 = c.adaptive_p2 != 0;
+        p.p2_alpha = c.p2_alpha;
+        p.p2_beta = c.p2_beta;
+        p.p2_lower_mult = c.p2_lower_mult;
+        p.p2_upper_mult = c.p2_upper_mult;
+        return p;
+    }
+
+    IOBuf* take_buf(Lane& L, int w, int h, std::map<std::pair<int, int>, int>& used)
+    {
+        auto& vec = L.pool[{w, h}];
+        int& k = used[{w, h}];
+        if ((int)vec.size() <= k) {
+            vec.emplace_back(new IOBuf());
+            vec.back()->alloc(w, h);
+        }
+        return vec[k++].get();
+    }
+
+    // Scheduler: whenever a lane is free and requests are queued, launch a batch.
+    void schedule()
+    {
+        for (;;) {
+            Lane* L = nullptr;
+            std::vector<Request*> batch;
+            bool fail_batch = false;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] {
+                    if (stop_) return true;
+                    if (queue_.empty()) return false;
+                    for (auto& l : lanes_)
+                        if (!l->busy) return true;
+                    return false;
+                });
+                if (stop_ && queue_.empty()) return;
+                for (auto& l : lanes_)
+                    if (!l->busy) { L = l.get(); break; }
+                if (!L) continue;
+                size_t bytes = 0;
+                while (!queue_.empty() && (int)batch.size() < max_batch_ && bytes + queue_.front()->bytes <= lane_budget_) {
+                    bytes += queue_.front()->bytes;
+                    batch.push_back(queue_.front());
+                    queue_.pop_front();
+                }
+                L->busy = true;
+                inflight_ += (int)batch.size();
+                max_inflight_pairs_ = std::max(max_inflight_pairs_, (long long)inflight_);
+                ++batches_;
+                batched_pairs_ += (long long)batch.size();
+                if (inject_ > 0) {
+                    --inject_;
+                    fail_batch = true;
+                }
+            }
+            L->reqs = batch;
+            L->bufs.clear();
+            L->error.clear();
+            try {
+                if (fail_batch) throw std::runtime_error("injected allocation failure");
+                launch(*L);
+            } catch (const std::exception& e) {
+                L->error = e.what();
+                cudaGetLastError();
+            }
+            cudaEventRecord(L->done, L->st);
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                pending_.push_back(L);
+            }
+            cv_.notify_all();
+        }
+    }
+
+    void launch(Lane& L)
+    {
+        std::map<std::pair<int, int>, int> used;
+        std::vector<pyrsgm_gb300_pair> pairs;
+        for (Request* q : L.reqs) {
+            const pyrsgm_gb300_request& r = q->r;
+            IOBuf* b = take_buf(L, r.width, r.height, used);
+            L.bufs.push_back(b);
+            const size_t px = (size_t)r.width * r.height;
+            std::memcpy(b->hL, r.h_left, px);
+            std::memcpy(b->hR, r.h_right, px);
+            if (cudaMemcpyAsync(b->dL, b->hL, px, cudaMemcpyHostToDevice, L.st) != cudaSuccess ||
+                cudaMemcpyAsync(b->dR, b->hR, px, cudaMemcpyHostToDevice, L.st) != cudaSuccess)
+                throw std::runtime_error("input copy failed");
+            pyrsgm_gb300_pair p{};
+            p.d_left = b->dL;
+            p.left_pitch = r.width;
+            p.d_right = b->dR;
+            p.right_pitch = r.width;
+            p.d_disp16 = r.h_disp16 ? b->d16 : nullptr;
+            p.disp16_pitch = (size_t)r.width * 2;
+            p.d_disp32 = r.h_disp32 ? b->d32 : nullptr;
+            p.disp32_pitch = (size_t)r.width * 4;
+            p.d_conf = r.h_conf ? b->dc : nullptr;
+            p.conf_pitch = (size_t)r.width * 4;
+            p.width = r.width;
+            p.height = r.height;
+            p.params = r.params;
+            pairs.push_back(p);
+        }
+        batch_engine_run(L.eng, pairs.data(), (int)pairs.size(), L.st, false);
+        for (size_t i = 0; i < L.reqs.size(); ++i) {
+            const pyrsgm_gb300_request& r = L.reqs[i]->r;
+            IOBuf* b = L.bufs[i];
+            const size_t px = (size_t)r.width * r.height;
+            if (r.h_disp16) cudaMemcpyAsync(b->h16, b->d16, px * 2, cudaMemcpyDeviceToHost, L.st);
+            if (r.h_disp32) cudaMemcpyAsync(b->h32, b->d32, px * 4, cudaMemcpyDeviceToHost, L.st);
+            if (r.h_conf) cudaMemcpyAsync(b->hc, b->dc, px * 4, cudaMemcpyDeviceToHost, L.st);
+        }
+    }
+
+    // Completion: lanes finish in launch order.
+    void complete()
+    {
+        for (;;) {
+            Lane* L = nullptr;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return !pending_.empty() || (stop_ && queue_.empty() && inflight_ == 0); });
+                if (pending_.empty()) return;
+                L = pending_.front();
+                pending_.pop_front();
+            }
+            const cudaError_t e = cudaEventSynchronize(L->done);
+            std::string err = L->error;
+            if (err.empty() && e != cudaSuccess) err = cudaGetErrorString(e);
+            if (err.empty()) {
+                const cudaError_t e2 = cudaStreamQuery(L->st);
+                if (e2 != cudaSuccess && e2 != cudaErrorNotReady) err = cudaGetErrorString(e2);
+            }
+            for (size_t i = 0; i < L->reqs.size() && err.empty(); ++i) {
+                const pyrsgm_gb300_request& r = L->reqs[i]->r;
+                IOBuf* b = L->bufs[i];
+                const size_t px = (size_t)r.width * r.height;
+                if (r.h_disp16) std::memcpy(r.h_disp16, b->h16, px * 2);
+                if (r.h_disp32) std::memcpy(r.h_disp32, b->h32, px * 4);
+                if (r.h_conf) std::memcpy(r.h_conf, b->hc, px * 4);
+            }
+            const double t = now_s();
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                for (Request* q : L->reqs) {
+                    q->t_done = t;
+                    if (err.empty()) {
+                        q->status = 1;
+                        ++ok_;
+                        lat_ms_.push_back((t - q->t_submit) * 1e3);
+                        last_done_ = t;
+                    } else {
+                        q->status = -1;
+                        q->error = err;
+                        ++failed_;
+                    }
+                }
+                inflight_ -= (int)L->reqs.size();
+                L->reqs.clear();
+                L->busy = false;
+            }
+            done_cv_.notify_all();
+            cv_.notify_all();
+        }
+    }
+
+    const int max_batch_, max_queue_;
+    size_t lane_budget_ = 0;
+    std::vector<std::unique_ptr<Lane>> lanes_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_cv_;
+    std::deque<Request*> queue_;
+    std::deque<Lane*> pending_;
+    std::unordered_map<long long, std::unique_ptr<Request>> all_;
+    long long next_id_ = 0;
+    int inflight_ = 0;
+    bool stop_ = false;
+    int inject_ = 0;
+    std::vector<double> lat_ms_;
+    long long ok_ = 0, failed_ = 0, refused_ = 0, batches_ = 0, batched_pairs_ = 0, max_inflight_pairs_ = 0;
+    double first_submit_ = 0, last_done_ = 0;
+    std::thread sched_, comp_;
+};
+
+}  // namespace pg
+
+namespace {
+void setErr(char* err, size_t len, const std::string& msg)
+{
+    if (err && len) {
+        std::strncpy(err, msg.c_str(), len - 1);
+        err[len - 1] = 0;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+void* pyrsgm_gb300_server_create(size_t device_budget_bytes, int max_batch, int num_streams, int max_queue, char* err,
+                                 size_t err_len)
+{
+    try {
+        return new pg::Server(device_budget_bytes, max_batch, num_streams, max_queue);
+    } catch (const std::exception& e) {
+        setErr(err, err_len, e.what());
+        return nullptr;
+    }
+}
+
+void pyrsgm_gb300_server_destroy(void* s) { delete static_cast<pg::Server*>(s); }
+
+long long pyrsgm_gb300_server_submit(void* s, const pyrsgm_gb300_request* r, char* err, size_t err_len)
+{
+    if (!s || !r) return -1;
+    std::string e;
+    const long long id = static_cast<pg::Server*>(s)->submit(*r, e);
+    if (id < 0) setErr(err, err_len, e);
+    return id;
+}
+
+int pyrsgm_gb300_server_wait(void* s, long long id, double timeout_s, char* err, size_t err_len)
+{
+    if (!s) return -1;
+    std::string e;
+    const int r = static_cast<pg::Server*>(s)->wait(id, timeout_s, e);
+    if (r < 0) setErr(err, err_len, e);
+    return r;
+}
+
+int pyrsgm_gb300_server_drain(void* s, double timeout_s) { return s ? static_cast<pg::Server*>(s)->drain(timeout_s) : -1; }
+
+int pyrsgm_gb300_server_stats(void* s, double* out10)
+{
+    if (!s || !out10) return -1;
+    static_cast<pg::Server*>(s)->stats(out10);
+    return 0;
+}
+
+void pyrsgm_gb300_server_reset_stats(void* s)
+{
+    if (s) static_cast<pg::Server*>(s)->reset_stats();
+}
+
+int pyrsgm_gb300_server_inject_failure(void* s, int batches)
+{
+    if (!s) return -1;
+    static_cast<pg::Server*>(s)->inject_failure(batches);
+    return 0;
+}
+
+}  // extern "C"
