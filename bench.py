@@ -165,6 +165,38 @@ class MineRunner:
         return int(lib().pyrsgm_gb300_launch_count())
 
 
+class BatchRunner(MineRunner):
+    """All pairs of a step in one BatchEngine run (one launch per stage and
+    kernel variant for the whole batch, replayed as a CUDA graph)."""
+
+    def __init__(self, pairs, dev):
+        super().__init__(pairs, dev)
+        pg = self.pg
+        self.engine = pg.BatchEngine(40 << 30)
+        items = [dict(left=self.L[i], right=self.R[i], params=pg.Params(**params_for(c)), disp16=self.d16[i],
+                      disp32=self.d32[i], conf=self.cf[i]) for i, c in enumerate(self.costs)]
+        self.arr = pg.BatchEngine.make_pairs(items)
+
+    def step(self, stream, pair_events=None):
+        self.engine.run_pairs(self.arr, True, stream)
+        if pair_events is not None:
+            for e in pair_events:
+                e.record(stream)
+
+    def step_direct(self, stream):
+        self.engine.run_pairs(self.arr, False, stream)
+
+    def step_e2e(self, stream):
+        for i in range(len(self.costs)):
+            self.L[i].copy_(self.hL[i], non_blocking=True)
+            self.R[i].copy_(self.hR[i], non_blocking=True)
+        self.engine.run_pairs(self.arr, True, stream)
+        for i in range(len(self.costs)):
+            self.h16[i].copy_(self.d16[i], non_blocking=True)
+            self.h32[i].copy_(self.d32[i], non_blocking=True)
+            self.hcf[i].copy_(self.cf[i], non_blocking=True)
+
+
 # ---------------------------------------------------------------------------
 # the reference's kernels (oracle/_ref) on the reference schedule
 # ---------------------------------------------------------------------------
@@ -282,6 +314,182 @@ def cpu_baseline(pairs, budget_s: float = 25.0) -> dict:
             "sample": f"{done} full 1920x1080 D=256 L3 pair(s) (Census first, then BT), adaptive P2 table from libm"}
 
 
+def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_timing: bool) -> dict:
+    """Warm up, then time args.steps device-resident steps (CUDA events on the
+    compute stream, L2 flushed between steps outside the events) and
+    args.steps // 2 end-to-end steps (host->device inputs, compute,
+    device->host outputs inside the events)."""
+    import torch
+    lib = None
+    graph = isinstance(runner, BatchRunner)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            runner.step(stream)
+    torch.cuda.synchronize()
+    if profile:
+        from pyrsgm_gb300._native import lib as _lib
+        lib = _lib()
+        if not graph:
+            lib.pyrsgm_gb300_profile(1)  # events around every launch of the timed steps
+    n0 = runner.launches()
+    step_ms, pair_ms = [], []
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.batch + 1)]
+                ev[0].record(stream)
+                runner.step(stream, ev[1:] if pair_timing else None)
+                if not pair_timing:
+                    ev[-1].record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(ev[0].elapsed_time(ev[-1]))
+            if pair_timing:
+                pair_ms += [ev[i].elapsed_time(ev[i + 1]) for i in range(args.batch)]
+    torch.cuda.synchronize()
+    launches = runner.launches() - n0
+    prof = {}
+    if lib is not None and graph:
+        # graph replays bypass the launchers: time the same launches of one
+        # step enqueued directly (events on the compute stream around each)
+        lib.pyrsgm_gb300_profile(1)
+        with torch.cuda.stream(stream):
+            flush.fill_(3)
+            runner.step_direct(stream)
+        torch.cuda.synchronize()
+    if lib is not None:
+        names = ["pyrdown", "features", "labels", "cost", "path_tb", "path_row", "post", "p2table"]
+        for k, nm in enumerate(names):
+            ms, cnt, by = C.c_double(), C.c_longlong(), C.c_double()
+            lib.pyrsgm_gb300_profile_read(k, C.byref(ms), C.byref(cnt), C.byref(by))
+            prof[nm] = {"ms": ms.value, "launches": cnt.value, "bytes": by.value}
+        lib.pyrsgm_gb300_profile(0)
+    total_ms = sum(step_ms)
+    e2e_ms = []
+    for _ in range(max(1, args.steps // 2)):
+        with torch.cuda.stream(stream):
+            flush.fill_(2)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            runner.step_e2e(stream)
+            b.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms.append(a.elapsed_time(b))
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([total_ms, e2e_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_total = float(t[0].item()), float(t[1].item())
+    return dict(total_ms=total_ms, step_ms=step_ms, pair_ms=pair_ms, launches=launches, prof=prof,
+                prof_steps=1 if graph else args.steps,
+                clocks=clk.summary(), e2e_total=e2e_total, e2e_steps=len(e2e_ms))
+
+
+def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, max_batch: int = 16,
+                  streams: int = 2, budget: int = 40 << 30) -> dict:
+    """n requests with Poisson arrivals at `rate` pairs/s, served (a) by the
+    continuous-batching server and (b) by plain sequential compute() of one
+    StereoMatcher per shape (one request at a time: H2D, compute, D2H).
+    Latency = arrival -> outputs in host memory."""
+    import numpy as np
+    import torch
+    import pyrsgm_gb300 as pg
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    picks = rng.integers(0, len(pairs_pool), n)
+    nout = max_batch * streams + 64
+
+    def outputs_for(w, h):
+        return [{"disp16": np.empty((h, w), np.int16), "disp32": np.empty((h, w), np.float32),
+                 "conf": np.empty((h, w), np.float32)} for _ in range(nout)]
+
+    shapes = {}
+    for l, _, c in pairs_pool:
+        shapes.setdefault((l.shape[1], l.shape[0]), None)
+    outs = {s: outputs_for(*s) for s in shapes}
+    # (a) server
+    srv = pg.Server(budget, max_batch=max_batch, streams=streams, max_queue=nout - max_batch * streams)
+    for k in range(min(4, n)):  # warm the pools
+        l, r, c = pairs_pool[picks[k]]
+        rid, _ = srv.submit(l, r, params_of(c), outputs=outs[(l.shape[1], l.shape[0])][k])
+        srv.wait(rid)
+    srv.reset_stats()
+    refused = 0
+    t0 = time.perf_counter()
+    for i in range(n):
+        dt = t0 + arrivals[i] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        l, r, c = pairs_pool[picks[i]]
+        try:
+            srv.submit(l, r, params_of(c), outputs=outs[(l.shape[1], l.shape[0])][i % nout])
+        except ValueError:
+            refused += 1
+    srv.drain()
+    st = srv.stats()
+    srv.close()
+    served = {"pairs_per_s": round(st["pairs_per_s"], 2), "p50_ms": round(st["p50_ms"], 3),
+              "p99_ms": round(st["p99_ms"], 3), "p999_ms": round(st["p999_ms"], 3),
+              "mean_batch": round(st["mean_batch"], 2), "completed": int(st["completed"]), "refused": refused}
+    # (b) plain sequential compute() on the same arrival stream
+    dev = torch.device("cuda")
+    matchers, bufs = {}, {}
+    for l, _, c in pairs_pool:
+        key = (l.shape[1], l.shape[0], c)
+        if key not in matchers:
+            w, h = key[0], key[1]
+            matchers[key] = pg.StereoMatcher(w, h, params_of(c))
+            bufs[(w, h)] = dict(L=torch.empty((h, w), dtype=torch.uint8, device=dev),
+                                R=torch.empty((h, w), dtype=torch.uint8, device=dev),
+                                d16=torch.empty((h, w), dtype=torch.int16, device=dev),
+                                d32=torch.empty((h, w), dtype=torch.float32, device=dev),
+                                cf=torch.empty((h, w), dtype=torch.float32, device=dev))
+    pinned = [(torch.from_numpy(l).pin_memory(), torch.from_numpy(r).pin_memory()) for l, r, _ in pairs_pool]
+    host_out = {s: (torch.empty((s[1], s[0]), dtype=torch.int16).pin_memory(),
+                    torch.empty((s[1], s[0]), dtype=torch.float32).pin_memory(),
+                    torch.empty((s[1], s[0]), dtype=torch.float32).pin_memory()) for s in shapes}
+    st = torch.cuda.Stream()
+    lat = []
+    t0 = time.perf_counter()
+    clock = 0.0
+    for i in range(n):
+        clock = max(clock, arrivals[i])
+        now = time.perf_counter() - t0
+        if now < clock:
+            time.sleep(clock - now)
+        k = picks[i]
+        l, r, c = pairs_pool[k]
+        w, h = l.shape[1], l.shape[0]
+        b = bufs[(w, h)]
+        with torch.cuda.stream(st):
+            b["L"].copy_(pinned[k][0], non_blocking=True)
+            b["R"].copy_(pinned[k][1], non_blocking=True)
+            matchers[(w, h, c)].compute_into(b["L"], b["R"], b["d16"], b["d32"], b["cf"], st)
+            ho = host_out[(w, h)]
+            ho[0].copy_(b["d16"], non_blocking=True)
+            ho[1].copy_(b["d32"], non_blocking=True)
+            ho[2].copy_(b["cf"], non_blocking=True)
+        st.synchronize()
+        done = time.perf_counter() - t0
+        lat.append((done - arrivals[i]) * 1e3)
+        clock = done
+    lat.sort()
+    plain = {"pairs_per_s": round(n / (clock - arrivals[0]), 2), "p50_ms": round(_pct(lat, 0.5), 3),
+             "p99_ms": round(_pct(lat, 0.99), 3), "p999_ms": round(_pct(lat, 0.999), 3)}
+    for m in matchers.values():
+        m.close()
+    return {"rate_pairs_per_s": rate, "requests": n, "max_batch": max_batch, "streams": streams,
+            "server": served, "plain_sequential": plain}
+
+
+def _pct(v, q):
+    s = sorted(v)
+    return s[max(0, min(len(s) - 1, int(round(q * (len(s) - 1)))))]
+
+
 def run(args) -> dict | None:
     import torch
     import torch.distributed as dist
@@ -295,101 +503,54 @@ def run(args) -> dict | None:
         return None
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-
-    pairs = make_inputs(args.batch)
-    Runner = MineRunner if args.impl == "mine" else ReferenceRunner
     if args.impl == "reference":
         from tests import _oracle
         if not _oracle.ref_available():
             print(json.dumps({"impl": "reference", "unavailable": "reference kernels (oracle/_ref) not built"}))
             return None
-    runner = Runner(pairs, dev)
+
+    pairs = make_inputs(args.batch)
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    pk = peaks()
+    npairs = args.batch * args.steps
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            runner.step(stream)
-    torch.cuda.synchronize()
-
-    # ---- device-resident throughput --------------------------------------
-    lib = None
-    if args.impl == "mine":
-        from pyrsgm_gb300._native import lib as _lib
-        lib = _lib()
-        lib.pyrsgm_gb300_profile(1)
-    n0 = runner.launches()
-    step_ms, pair_ms = [], []
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(1)
-                ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.batch + 1)]
-                ev[0].record(stream)
-                runner.step(stream, ev[1:])
-            torch.cuda.synchronize()
-            step_ms.append(ev[0].elapsed_time(ev[-1]))
-            pair_ms += [ev[i].elapsed_time(ev[i + 1]) for i in range(args.batch)]
-    torch.cuda.synchronize()
-    launches = runner.launches() - n0
-    prof = {}
-    if lib is not None:
-        names = ["pyrdown", "features", "labels", "cost", "path_tb", "path_row", "post", "p2table"]
-        for k, nm in enumerate(names):
-            ms, cnt, by = C.c_double(), C.c_longlong(), C.c_double()
-            lib.pyrsgm_gb300_profile_read(k, C.byref(ms), C.byref(cnt), C.byref(by))
-            prof[nm] = {"ms": ms.value, "launches": cnt.value, "bytes": by.value}
-        lib.pyrsgm_gb300_profile(0)
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.batch * args.steps / (total_ms / 1e3)
-
-    # ---- end to end through the public API -------------------------------
-    e2e_ms = []
-    for _ in range(max(1, args.steps // 2)):
-        with torch.cuda.stream(stream):
-            flush.fill_(2)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            runner.step_e2e(stream)
-            b.record(stream)
-        torch.cuda.synchronize()
-        e2e_ms.append(a.elapsed_time(b))
-    e2e_total = sum(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * args.batch * len(e2e_ms) / (e2e_total / 1e3)
-
+    if args.impl == "reference":
+        m = measure(ReferenceRunner(pairs, dev), args, stream, flush, dev, 1, dist, False, True)
+        headline, plain = m, m
+    else:
+        plain = measure(MineRunner(pairs, dev), args, stream, flush, dev, world, dist, False, True)
+        headline = plain if args.mode == "plain" else \
+            measure(BatchRunner(pairs, dev), args, stream, flush, dev, world, dist, True, False)
+        if args.mode == "plain":
+            headline = measure(MineRunner(pairs, dev), args, stream, flush, dev, world, dist, True, True)
+    value = world * npairs / (headline["total_ms"] / 1e3)
+    e2e_value = world * args.batch * headline["e2e_steps"] / (headline["e2e_total"] / 1e3)
     if rank != 0:
         return None
-    pk = peaks()
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int16", "data": "synthetic (seeded value-noise pairs, "
-        "slanted-plane Voronoi ground truth; stands in for Middlebury)",
+        "warmup": args.warmup, "ms_per_step": round(headline["total_ms"] / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+        "data": "synthetic (seeded value-noise pairs, slanted-plane Voronoi ground truth; stands in for Middlebury)",
         "config": {"workload": "1920x1080 D=256 pyramid_levels=3, Census/BT alternating, adaptive P2, median, "
                    "disp16+disp32+conf", "pairs_per_step": args.batch, "width": W, "height": H,
                    "num_disparities": D, "pyramid_levels": LEVELS, "l2": "flushed (256 MB write) between steps",
-                   "parallelism": f"replicas x{world}"},
-        "latency_ms": {"p50": round(statistics.median(pair_ms), 4),
-                       "p99": round(sorted(pair_ms)[max(0, int(len(pair_ms) * 0.99) - 1)], 4),
-                       "unit": "per pair, back-to-back compute() on one stream"},
+                   "parallelism": f"replicas x{world}",
+                   "execution": "plain per-pair compute()" if (args.mode == "plain" or args.impl == "reference")
+                   else "batched: one BatchEngine run per step (CUDA graph)"},
         "e2e": {"value": round(e2e_value, 3), "unit": "pairs/s",
                 "h2d_bytes_per_step": args.batch * 2 * W * H,
                 "d2h_bytes_per_step": args.batch * W * H * (2 + 4 + 4)},
-        "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "gpu_launches": headline["launches"],
+        "clocks": headline["clocks"],
     }
+    if plain["pair_ms"]:
+        out["plain_compute"] = {"value": round(world * npairs / (plain["total_ms"] / 1e3), 3), "unit": "pairs/s",
+                                "latency_ms_p50": round(_pct(plain["pair_ms"], 0.5), 4),
+                                "latency_ms_p99": round(_pct(plain["pair_ms"], 0.99), 4)}
     if args.impl == "mine":
+        prof = headline["prof"]
         row = prof.get("path_row", {})
         achieved = (row["bytes"] / (row["ms"] / 1e3) / 1e9) if row.get("ms") else None
         out["roofline"] = {"kernel": "k_path_row (L->R + R->L + WTA + disp2 + LR check)", "bound": "hbm",
@@ -397,15 +558,45 @@ def run(args) -> dict | None:
                            "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4) if achieved else None,
                            "peak_source": pk["source"], "traffic": None,
                            "avg_launch_ms": round(row["ms"] / row["launches"], 5) if row.get("launches") else None}
-        out["kernels_ms_per_step"] = {k: round(v["ms"] / args.steps, 4) for k, v in prof.items() if v["launches"]}
-        if not args.no_cpu and world == 1:
-            out["cpu_baseline"] = cpu_baseline(pairs)
+        out["kernels_ms_per_step"] = {k: round(v["ms"] / headline["prof_steps"], 4)
+                                      for k, v in prof.items() if v["launches"]}
     else:
         out["impl"] = "reference"
         out["reference_build"] = "reference src/sgm_kernels.cu + src/pyrdown.cu compiled unmodified for sm_103a"
-        if not args.no_cpu and world == 1:
-            out["cpu_baseline"] = cpu_baseline(pairs)
+    if args.impl == "mine" and world == 1 and args.serve_requests > 0:
+        import pyrsgm_gb300 as pg
+        rate = round(0.7 * value, 1)
+        out["serving"] = serve_compare(pairs, lambda c: pg.Params(**params_for(c)), rate, args.serve_requests)
+    if not args.no_cpu and world == 1:
+        out["cpu_baseline"] = cpu_baseline(pairs)
     return out
+
+
+MIX_SIZES = [(640, 480), (960, 540), (1280, 720), (1920, 1080)]
+
+
+def serve_sweep(args) -> None:
+    """Serving on the mixed stream (sizes 640x480..1920x1080, D in {64,128,256},
+    pyramid levels 1-4, Census/BT): one JSON line per arrival rate."""
+    import numpy as np
+    import torch
+    import pyrsgm_gb300 as pg
+    from pyrsgm_gb300 import synth
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(4000)
+    pool, cfg = [], []
+    for i in range(args.pool):
+        w, h = MIX_SIZES[rng.integers(len(MIX_SIZES))]
+        D = int(rng.choice([64, 128, 256]))
+        L = int(rng.integers(1, 5))
+        c = int(rng.integers(2))
+        left, right, _ = synth.make_pair(w, h, D - 1, 10, 4000 + i)
+        pool.append((left, right, i))
+        cfg.append(pg.Params(num_disparities=D, pyramid_levels=L, cost_mode=c, p1=8 if c else 300,
+                             p2=32 if c else 2400))
+    for rate in args.rates:
+        res = serve_compare(pool, lambda k: cfg[k], rate, args.serve_requests, seed=int(rate))
+        print(json.dumps({"metric": "mixed-stream serving", **res}), flush=True)
 
 
 def main():
@@ -415,10 +606,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=8, help="pairs per step")
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--mode", choices=["batched", "plain", "serve"], default="batched",
+                    help="headline execution: one batched run per step, or per-pair compute(); "
+                         "'serve' sweeps arrival rates on the mixed-size stream")
+    ap.add_argument("--serve-requests", type=int, default=160,
+                    help="requests of the serving comparison (0 skips it)")
+    ap.add_argument("--rates", type=float, nargs="*", default=[500, 1000, 2000, 5000, 10000, 20000])
+    ap.add_argument("--pool", type=int, default=24, help="distinct pairs of the serving sweep")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.mode == "serve":
+        serve_sweep(args)
+        return
     out = run(args)
     if out is not None:
         print(json.dumps(out))

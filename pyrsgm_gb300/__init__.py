@@ -5,9 +5,9 @@ include/pyrsgm/); this package builds it (pyrsgm_gb300.build) and exposes a
 thin Python surface over it (pyrsgm_gb300.api).
 """
 from .api import (COST_BT, COST_CENSUS, POST_LRCHECK, POST_MEDIAN, BatchEngine, LevelInfo, Params,
-                  StereoMatcher, Workspace, pair_bytes, compute_level, compute_single_scale, invalid_disparity16, level_geometry,
+                  Server, StereoMatcher, Workspace, pair_bytes, compute_level, compute_single_scale, invalid_disparity16, level_geometry,
                   pyrdown, validate_params)
 
-__all__ = ["COST_BT", "COST_CENSUS", "POST_LRCHECK", "POST_MEDIAN", "BatchEngine", "LevelInfo", "pair_bytes", "Params", "StereoMatcher",
+__all__ = ["COST_BT", "COST_CENSUS", "POST_LRCHECK", "POST_MEDIAN", "BatchEngine", "LevelInfo", "pair_bytes", "Server", "Params", "StereoMatcher",
            "Workspace", "compute_level", "compute_single_scale", "invalid_disparity16", "level_geometry", "pyrdown",
            "validate_params"]

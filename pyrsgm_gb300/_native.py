@@ -36,6 +36,12 @@ class Pair(C.Structure):
                 ("d_conf", _vp), ("conf_pitch", _sz), ("width", _i), ("height", _i), ("params", Params)]
 
 
+class Request(C.Structure):
+    """pyrsgm_gb300_request: one served pair (host buffers, pitch = width)."""
+    _fields_ = [("h_left", _vp), ("h_right", _vp), ("h_disp16", _vp), ("h_disp32", _vp), ("h_conf", _vp),
+                ("width", _i), ("height", _i), ("params", Params)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "pyrsgm_create_workspace": (_vp, []),
@@ -74,6 +80,14 @@ _SIGS = {
     "pyrsgm_gb300_batch_run": (_i, [_vp, C.POINTER(Pair), _i, _i, _vp, C.c_char_p, _sz]),
     "pyrsgm_gb300_batch_bytes_in_use": (_sz, [_vp]),
     "pyrsgm_gb300_pair_bytes": (_sz, [_i, _i, C.POINTER(Params)]),
+    "pyrsgm_gb300_server_create": (_vp, [_sz, _i, _i, _i, C.c_char_p, _sz]),
+    "pyrsgm_gb300_server_destroy": (None, [_vp]),
+    "pyrsgm_gb300_server_submit": (C.c_longlong, [_vp, C.POINTER(Request), C.c_char_p, _sz]),
+    "pyrsgm_gb300_server_wait": (_i, [_vp, C.c_longlong, C.c_double, C.c_char_p, _sz]),
+    "pyrsgm_gb300_server_drain": (_i, [_vp, C.c_double]),
+    "pyrsgm_gb300_server_stats": (_i, [_vp, C.POINTER(C.c_double)]),
+    "pyrsgm_gb300_server_reset_stats": (None, [_vp]),
+    "pyrsgm_gb300_server_inject_failure": (_i, [_vp, _i]),
     "pyrsgm_gb300_version": (C.c_char_p, []),
     "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
     "pyrsgm_gb300_profile": (_i, [_i]),

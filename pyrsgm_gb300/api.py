@@ -242,6 +242,78 @@ class BatchEngine:
     __del__ = close
 
 
+class Server:
+    """Continuous-batching server (pyrsgm_gb300_server_*) over host buffers.
+
+    submit() takes uint8 numpy images and returns (request id, outputs dict);
+    the outputs are filled when wait(id) returns 1.
+    """
+
+    STATS = ("completed", "failed", "p50_ms", "p99_ms", "p999_ms", "mean_batch", "pairs_per_s", "peak_inflight",
+             "refused", "max_ms")
+
+    def __init__(self, budget_bytes: int, max_batch: int = 16, streams: int = 2, max_queue: int = 4096):
+        err = C.create_string_buffer(256)
+        self._h = lib().pyrsgm_gb300_server_create(budget_bytes, max_batch, streams, max_queue, err, 256)
+        if not self._h:
+            raise RuntimeError(err.value.decode())
+        self._keep: dict[int, tuple] = {}
+
+    def submit(self, left, right, params: Params, want16: bool = True, want32: bool = False,
+               want_conf: bool = False, outputs: dict | None = None):
+        import numpy as np
+        h, w = left.shape
+        left = np.ascontiguousarray(left, dtype=np.uint8)
+        right = np.ascontiguousarray(right, dtype=np.uint8)
+        out = outputs if outputs is not None else {
+            "disp16": np.empty((h, w), np.int16) if want16 else None,
+            "disp32": np.empty((h, w), np.float32) if want32 else None,
+            "conf": np.empty((h, w), np.float32) if want_conf else None}
+        r = _native.Request()
+        r.h_left, r.h_right = left.ctypes.data, right.ctypes.data
+        r.h_disp16 = out["disp16"].ctypes.data if out.get("disp16") is not None else None
+        r.h_disp32 = out["disp32"].ctypes.data if out.get("disp32") is not None else None
+        r.h_conf = out["conf"].ctypes.data if out.get("conf") is not None else None
+        r.width, r.height = w, h
+        r.params = params.to_c()
+        err = C.create_string_buffer(256)
+        rid = lib().pyrsgm_gb300_server_submit(self._h, C.byref(r), err, 256)
+        if rid < 0:
+            raise ValueError(err.value.decode())
+        self._keep[rid] = (left, right, out)
+        return rid, out
+
+    def wait(self, rid: int, timeout: float = -1.0) -> int:
+        err = C.create_string_buffer(256)
+        s = lib().pyrsgm_gb300_server_wait(self._h, rid, timeout, err, 256)
+        if s != 0:
+            self._keep.pop(rid, None)
+        if s < 0:
+            self.last_error = err.value.decode()
+        return s
+
+    def drain(self, timeout: float = -1.0) -> bool:
+        return lib().pyrsgm_gb300_server_drain(self._h, timeout) == 1
+
+    def stats(self) -> dict:
+        o = (C.c_double * 10)()
+        lib().pyrsgm_gb300_server_stats(self._h, o)
+        return dict(zip(self.STATS, list(o)))
+
+    def reset_stats(self) -> None:
+        lib().pyrsgm_gb300_server_reset_stats(self._h)
+
+    def inject_failure(self, batches: int) -> None:
+        lib().pyrsgm_gb300_server_inject_failure(self._h, batches)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().pyrsgm_gb300_server_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+
 class Workspace:
     """Opaque C-API workspace (pyrsgm_create_workspace / destroy)."""
 
