@@ -313,8 +313,7 @@ private:
                               return launch_cost(b, e, s);
                           }, st, "cost");
             launchGrouped(jobs, [](const LevelDesc& d) {
-                const PathShape ps = path_shape(d.D);
-                return d.pyr * 100000 + ps.G * 1000 + ps.K;
+                return d.pyr * 100000 + path_variant(d.D);
             }, [](const Jobs<kBatchJobs>& b, const LevelExtent& e, cudaStream_t s) {
                 return launch_paths(b, e, s);
             }, st, "aggregation");

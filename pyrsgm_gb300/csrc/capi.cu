@@ -32,7 +32,7 @@ size_t Workspace::bytes_for(int w, int h, int D)
 {
     const size_t px = (size_t)w * h;
     return align256(px * 8) * 2 + align256(px * 2) + align256(px * D * 2) * 2 + align256(px * 2) +
-           align256(px * 4) + align256(256 * 4);
+           align256(px * 4) * 2 + align256(256 * 4);
 }
 
 int Workspace::ensure(int w, int h, int D)
@@ -61,6 +61,7 @@ void Workspace::carve(unsigned char* p, int w, int h, int D)
     V = reinterpret_cast<int16_t*>(p); p += align256(px * D * 2);
     disp_raw = reinterpret_cast<int16_t*>(p); p += align256(px * 2);
     conf_raw = reinterpret_cast<float*>(p); p += align256(px * 4);
+    keys = reinterpret_cast<unsigned*>(p); p += align256(px * 4);
     lut = reinterpret_cast<int*>(p);
     width = w; height = h; disp = D;
 }
@@ -92,6 +93,7 @@ void fill_workspace_ptrs(LevelDesc& d, const Workspace& ws)
     d.V = ws.V;
     d.disp_raw = ws.disp_raw;
     d.conf_raw = ws.conf_raw;
+    d.keys = ws.keys;
     d.p2lut = ws.lut;
     d.debug_acc = ws.debug & PYRSGM_GB300_DEBUG_AGGREGATED;
 }

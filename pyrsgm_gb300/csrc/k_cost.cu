@@ -122,6 +122,7 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
         f.y = interval(px(y, x), px(y, xm), px(y, xq));
     }
     feat[(size_t)y * W + x] = f;
+    if (view == 0) J.keys[(size_t)y * W + x] = 0xffffffffu;  // no disp2 candidate yet
 }
 
 // ---------------------------------------------------------------------------
@@ -334,6 +335,120 @@ __global__ void __launch_bounds__(256) k_cost_bt_local(const __grid_constant__ J
 }
 
 // ---------------------------------------------------------------------------
+// BT refine cost, tiled.  Same values as k_cost_bt_local, computed per
+// 32x8 tile from the BT costs of every (window pixel, real disparity) pair
+// the tile needs: the real disparities of a tile are
+// [min base, max base + D - 1]; when that span is at most kTiRn, the BT
+// cost of each (clamped window pixel, real disparity) is evaluated once into
+// shared memory, summed along x, then along y, and each voxel picks the sum
+// at its own real disparity.  Window sums are exact integers (no
+// intermediate clamp in the reference) and clamped to kMax - 1 at the end.
+// Tiles whose parents disagree more widely fall back to direct evaluation.
+// ---------------------------------------------------------------------------
+constexpr int kTiX = 32, kTiY = 8, kTiRn = 32, kTiMaxHalf = 2;
+
+template <int NJ>
+__global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ Jobs<NJ> jobs)
+{
+    const LevelDesc& J = jobs.d[blockIdx.z];
+    const int x0 = blockIdx.x * kTiX, y0 = blockIdx.y * kTiY;
+    if (x0 >= J.w || y0 >= J.h) return;
+    const int W = J.w, H = J.h, D = J.D, h = J.bs / 2;
+    constexpr int SW = kTiX + 2 * kTiMaxHalf, SH = kTiY + 2 * kTiMaxHalf;
+    __shared__ uint8_t bt[SH][SW][kTiRn];            // BT cost per (row, col, r - rmin)
+    __shared__ uint16_t hs[SH][kTiX][kTiRn];         // sums along x
+    __shared__ int16_t sbase[kTiY][kTiX];
+    __shared__ int red[2];
+    const int tid = threadIdx.x;
+    const int tx = tid & (kTiX - 1), ty = tid / kTiX;
+    const int x = x0 + tx, y = y0 + ty;
+    const bool inside = x < W && y < H;
+    int b = kNoParent;
+    if (inside) b = J.base[(size_t)y * W + x];
+    sbase[ty][tx] = (int16_t)b;
+    if (tid == 0) { red[0] = INT_MAX; red[1] = INT_MIN; }
+    __syncthreads();
+    if (inside && b != kNoParent) {
+        atomicMin(&red[0], b);
+        atomicMax(&red[1], b);
+    }
+    __syncthreads();
+    const int rmin = red[0], rmax = red[1] + D - 1;
+    const bool tiled = red[1] != INT_MIN && rmax - rmin + 1 <= kTiRn && h <= kTiMaxHalf;
+    if (tiled) {
+        const int rn = rmax - rmin + 1;
+        const int sw = kTiX + 2 * h, sh = kTiY + 2 * h;
+        for (int i = tid; i < sh * sw * rn; i += blockDim.x) {
+            const int ri = i % rn;
+            const int j = (i / rn) % sw;
+            const int r = i / (rn * sw);
+            const int gy = iclamp(y0 - h + r, 0, H - 1), gx = iclamp(x0 - h + j, 0, W - 1);
+            const int x2 = gx - (rmin + ri);
+            int v = 255;
+            if (x2 >= 0 && x2 < W) v = bt_pixel(J.featL[(size_t)gy * W + gx], J.featR[(size_t)gy * W + x2]);
+            bt[r][j][ri] = (uint8_t)v;
+        }
+        __syncthreads();
+        for (int i = tid; i < sh * kTiX * rn; i += blockDim.x) {
+            const int ri = i % rn;
+            const int j = (i / rn) % kTiX;
+            const int r = i / (rn * kTiX);
+            int s = 0;
+            for (int k = 0; k <= 2 * h; ++k) s += bt[r][j + k][ri];
+            hs[r][j][ri] = (uint16_t)s;
+        }
+        __syncthreads();
+        // one (pixel, label) per thread and pass: consecutive threads write consecutive labels
+        for (int i = tid; i < kTiX * kTiY * D; i += blockDim.x) {
+            const int d = i % D;
+            const int px = (i / D) % kTiX;
+            const int py = i / (D * kTiX);
+            const int xx = x0 + px, yy = y0 + py;
+            if (xx >= W || yy >= H) continue;
+            const int base = sbase[py][px];
+            int lo, hi;
+            label_range(J, xx, base, lo, hi);
+            int out = kMax;
+            if (d >= lo && d <= hi) {
+                const int ri = base + d - rmin;
+                int s = 0;
+                for (int k = 0; k <= 2 * h; ++k) s += hs[py + k][px][ri];
+                out = imin(s, kMax - 1);
+            }
+            J.C[((size_t)yy * W + xx) * D + d] = (int16_t)out;
+        }
+    } else {
+        for (int i = tid; i < kTiX * kTiY * D; i += blockDim.x) {
+            const int d = i % D;
+            const int px = (i / D) % kTiX;
+            const int py = i / (D * kTiX);
+            const int xx = x0 + px, yy = y0 + py;
+            if (xx >= W || yy >= H) continue;
+            const int base = sbase[py][px];
+            int lo, hi;
+            label_range(J, xx, base, lo, hi);
+            int out = kMax;
+            if (d >= lo && d <= hi) {
+                const int real = base + d;
+                int sum = 0;
+                for (int dy = -h; dy <= h; ++dy) {
+                    const int gy = iclamp(yy + dy, 0, H - 1);
+                    const uint2* lrow = J.featL + (size_t)gy * W;
+                    const uint2* rrow = J.featR + (size_t)gy * W;
+                    for (int dx = -h; dx <= h; ++dx) {
+                        const int gx = iclamp(xx + dx, 0, W - 1);
+                        const int x2 = gx - real;
+                        sum += (x2 >= 0 && x2 < W) ? bt_pixel(__ldg(&lrow[gx]), __ldg(&rrow[x2])) : 255;
+                    }
+                }
+                out = imin(sum, kMax - 1);
+            }
+            J.C[((size_t)yy * W + xx) * D + d] = (int16_t)out;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
 template <int NB>
@@ -395,8 +510,8 @@ cudaError_t launch_cost(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t
         dim3 g((unsigned)((n + 255) / 256), jobs.n);
         k_cost_census<NJ><<<g, 256, 0, st>>>(jobs);
     } else if (J0.refine) {
-        dim3 g((unsigned)((e.max_vox + 255) / 256), jobs.n);
-        k_cost_bt_local<NJ><<<g, 256, 0, st>>>(jobs);
+        dim3 g((e.max_w + kTiX - 1) / kTiX, (e.max_h + kTiY - 1) / kTiY, jobs.n);
+        k_cost_bt_tiled<NJ><<<g, 256, 0, st>>>(jobs);
     } else {
         int maxHalf = 0;
         for (int j = 0; j < jobs.n; ++j) maxHalf = std::max(maxHalf, jobs.d[j].bs / 2);

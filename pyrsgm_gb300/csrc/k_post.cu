@@ -38,8 +38,35 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
     if (x >= J.w || y >= J.h) return;
     const int W = J.w, H = J.h;
     const size_t p = (size_t)y * W + x;
-    int d = J.disp_raw[p];
-    float c = J.conf_raw[p];
+    const int16_t inv = (int16_t)((J.minD - 1) * 16);
+    // Levels aggregated by the packed kernels leave the LR check to this
+    // pass (kernel_StrictPyramidLRCheck / kernel_PseudoLRCheck,
+    // src/sgm_kernels.cu:825-889), applied to every pixel the median reads.
+    const bool check = uses_packed(J.D) && (J.post & POST_LRCHECK);
+    auto disp_at = [&](int xx, int yy) -> int {
+        const int d16 = J.disp_raw[(size_t)yy * W + xx];
+        if (!check || d16 == inv) return d16;
+        const unsigned* krow = J.keys + (size_t)yy * W;
+        auto disp2 = [&](int rx) -> int {
+            const unsigned k = krow[rx];
+            return k == 0xffffffffu ? (int)inv : (int)(0xffffu - (k & 0xffffu)) - rx;
+        };
+        const int d0 = d16 >> 4, d1 = (d16 + 15) >> 4;
+        const int r0 = xx - d0, r1 = xx - d1;
+        if (J.pyr) {
+            bool ok = false;
+            if (r0 >= 0 && r0 < W) { const int v = disp2(r0); if (v >= J.minD && abs(v - d0) <= J.maxdiff) ok = true; }
+            if (r1 >= 0 && r1 < W) { const int v = disp2(r1); if (v >= J.minD && abs(v - d1) <= J.maxdiff) ok = true; }
+            return ok ? d16 : (int)inv;
+        }
+        bool bad0 = false, bad1 = false;
+        if (r0 >= 0 && r0 < W) { const int v = disp2(r0); bad0 = v >= J.minD && abs(v - d0) > J.maxdiff; }
+        if (r1 >= 0 && r1 < W) { const int v = disp2(r1); bad1 = v >= J.minD && abs(v - d1) > J.maxdiff; }
+        return (bad0 && bad1) ? (int)inv : d16;
+    };
+    const int d_in = J.disp_raw[p];
+    int d = disp_at(x, y);
+    float c = (d != d_in) ? 0.0f : J.conf_raw[p];  // the check zeroes what it rejects
     if (J.post & POST_MEDIAN) {
         int v[9];
         int n = 0;
@@ -49,7 +76,7 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
             for (int dx = -1; dx <= 1; ++dx) {
                 const int xx = x + dx;
                 if (xx < 0 || xx >= W) continue;
-                v[n++] = J.disp_raw[(size_t)yy * W + xx];
+                v[n++] = (dx == 0 && dy == 0) ? d : disp_at(xx, yy);
             }
         }
         for (int i = 1; i < n; ++i) {
@@ -64,7 +91,6 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
     }
     if (J.out16) J.out16[(size_t)y * J.out16_pitch + x] = (int16_t)d;
     if (J.out32 && J.outc) {
-        const int16_t inv = (int16_t)((J.minD - 1) * 16);
         const float f = (int16_t)d / 16.0f;
         const bool ok = (int16_t)d != inv && f > 0.0f;
         J.out32[(size_t)y * J.out32_pitch + x] = ok ? f : 0.0f;

@@ -41,6 +41,7 @@ struct LevelDesc {
     int16_t* V;
     int16_t* disp_raw;
     float* conf_raw;
+    unsigned* keys;   // disp2 candidates: (cost << 16 | 0xFFFF - x) per right-image pixel
     const int* p2lut;
     // outputs (device, optional)
     int16_t* out16;
@@ -67,6 +68,10 @@ struct Jobs {
     LevelDesc d[NJ];
     int n;
 };
+
+// Label counts aggregated by the thread-per-chain packed kernels
+// (k_paths_packed.cuh); their LR check runs in the post kernel.
+__host__ __device__ __forceinline__ bool uses_packed(int D) { return D == 16 || D == 32 || D == 64; }
 
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }

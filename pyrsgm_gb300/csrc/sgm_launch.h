@@ -74,6 +74,15 @@ struct PathShape {
     int G, K;
 };
 PathShape path_shape(int D);
+// Kernel family of a label count: 10000 + D for the thread-per-chain packed
+// kernels, else G * 100 + K of the lane-parallel ones.  Jobs of one
+// aggregation launch share it.
+inline int path_variant(int D)
+{
+    if (uses_packed(D)) return 10000 + D;
+    const PathShape s = path_shape(D);
+    return s.G * 100 + s.K;
+}
 
 // Count of kernel launches issued by this library (process-wide); a CUDA
 // graph replay counts the kernels it contains.

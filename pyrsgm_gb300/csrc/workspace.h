@@ -6,6 +6,7 @@
 //   V             int16  [h][w][D]  aggregation volume
 //   disp_raw      int16  [h][w]     disparity*16 before the median
 //   conf_raw      float  [h][w]     confidence before the median reset
+//   keys          u32    [h][w]     disp2 candidates (cost << 16 | 0xFFFF - x)
 //   lut           int    [256]      adaptive-P2 table
 #pragma once
 
@@ -31,6 +32,7 @@ struct Workspace {
     int16_t* V = nullptr;
     int16_t* disp_raw = nullptr;
     float* conf_raw = nullptr;
+    unsigned* keys = nullptr;
     int* lut = nullptr;
 
     static size_t bytes_for(int w, int h, int D);
