@@ -361,7 +361,7 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
             runner.step_direct(stream)
         torch.cuda.synchronize()
     if lib is not None:
-        names = ["pyrdown", "features", "labels", "cost", "path_tb", "path_row", "post", "p2table"]
+        names = ["pyrdown", "features", "labels", "cost", "path_tb", "path_row", "post", "p2table", "wta"]
         for k, nm in enumerate(names):
             ms, cnt, by = C.c_double(), C.c_longlong(), C.c_double()
             lib.pyrsgm_gb300_profile_read(k, C.byref(ms), C.byref(cnt), C.byref(by))

@@ -180,7 +180,8 @@ unsigned long long pyrsgm_gb300_launch_count(void);
  * pyrsgm_gb300_profile(1) clears the records and starts recording,
  * pyrsgm_gb300_profile(0) stops.  _read() waits for the recorded events of
  * one kernel kind (0 pyrDown, 1 features, 2 refine labels, 3 cost volume,
- * 4 top->bottom path, 5 row pass, 6 post, 7 P2 table) and returns the summed
+ * 4 top->bottom path, 5 row pass, 6 post, 7 P2 table, 8 winner-take-all of
+ * the 16/32/64-label levels) and returns the summed
  * device time in ms, the launch count and the summed algorithmic bytes. */
 int pyrsgm_gb300_profile(int enable);
 int pyrsgm_gb300_profile_read(int kind, double* ms_total, long long* launches, double* bytes_total);

@@ -184,39 +184,47 @@ __global__ void k_p2_table(int* lut, int P2, float alpha, float beta, float lowe
 // Census cost volume.  Coarse / single-scale: kernel_CensusCost
 // (src/sgm_kernels.cu:303-327), 24 when x - d - minD is outside the image.
 // Refine: kernel_CensusCostLocal (src/sgm_kernels.cu:1112-1133), kMax for a
-// geometry-invalid label.  Each thread writes two labels (one 32-bit store).
+// geometry-invalid label.  One thread per pixel writes its D labels, eight
+// per 16-byte store (label pairs or single labels when D is not a multiple
+// of eight).
 // ---------------------------------------------------------------------------
 template <int NJ>
 __global__ void __launch_bounds__(256) k_cost_census(const __grid_constant__ Jobs<NJ> jobs)
 {
-    const LevelDesc& J = jobs.d[blockIdx.y];
-    const int half = J.D >> 1;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)J.w * J.h * half;
-    if (i >= total) return;
-    const int pair = (int)(i % half);
-    const long long p = i / half;
-    const int y = (int)(p / J.w), x = (int)(p - (long long)y * J.w);
+    const LevelDesc& J = jobs.d[blockIdx.z];
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= J.w || y >= J.h) return;
+    const int W = J.w, D = J.D;
+    const size_t p = (size_t)y * W + x;
     const uint32_t cl = J.featL[p].x;
-    const uint2* rrow = J.featR + (size_t)y * J.w;
-    int c[2];
+    const uint2* rrow = J.featR + (size_t)y * W;
+    // label d reads right pixel x - off - d when lo <= d <= hi, else `fill`
+    int off, lo, hi, fill;
     if (J.refine) {
-        const int base = J.base[p];
-        int lo, hi;
-        label_range(J, x, base, lo, hi);
+        off = J.base[p];
+        label_range(J, x, off, lo, hi);
+        fill = kMax;
+    } else {
+        off = J.minD;
+        lo = imax(0, x - off - (W - 1));
+        hi = imin(D - 1, x - off);
+        fill = 24;
+    }
+    auto cost = [&](int d) -> uint32_t {
+        return (d >= lo && d <= hi) ? (uint32_t)__popc(cl ^ __ldg(&rrow[x - off - d].x)) : (uint32_t)fill;
+    };
+    int16_t* out = J.C + p * D;
+    if ((D & 7) == 0) {
+        for (int d0 = 0; d0 < D; d0 += 8) {
+            uint32_t w[4];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const int d = 2 * pair + k;
-            c[k] = (d >= lo && d <= hi) ? __popc(cl ^ rrow[x - (base + d)].x) : kMax;
+            for (int i = 0; i < 4; ++i) w[i] = cost(d0 + 2 * i) | (cost(d0 + 2 * i + 1) << 16);
+            reinterpret_cast<uint4*>(out + d0)[0] = make_uint4(w[0], w[1], w[2], w[3]);
         }
     } else {
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const int x2 = x - (2 * pair + k + J.minD);
-            c[k] = (x2 >= 0 && x2 < J.w) ? __popc(cl ^ rrow[x2].x) : 24;
-        }
+        for (int d = 0; d < D; ++d) out[d] = (int16_t)cost(d);
     }
-    reinterpret_cast<uint32_t*>(J.C + p * J.D)[pair] = (uint32_t)(uint16_t)c[0] | ((uint32_t)(uint16_t)c[1] << 16);
 }
 
 // BT cost of one (left pixel, right pixel) pair from packed features:
@@ -298,54 +306,57 @@ __global__ void __launch_bounds__(256) k_cost_bt_box(const __grid_constant__ Job
 
 // ---------------------------------------------------------------------------
 // BT refine cost: kernel_BTWindowCostLocal, src/sgm_kernels.cu:1075-1110.
-// Direct blockSize^2 window of BT pixel costs at the real disparity
-// base + d over clamped pixels; kMax for a geometry-invalid label; the sum
-// is clamped to kMax - 1.  One thread per (pixel, label).
+// For label d of pixel p the reference sums, over the blockSize^2 window of
+// clamped pixels q, the BT cost of q at the real disparity base_p + d (255
+// when q - (base_p + d) leaves the image), clamps the sum to kMax - 1, and
+// writes kMax for a geometry-invalid label.  The sum depends on p only
+// through the window and the real disparity, so one 32x8 tile evaluates
+// each (window pixel, real disparity) pair once when the real disparities
+// its pixels need, [min base, max base + D - 1], span at most kTiRn:
+//   phase 1: a warp walks a window row left to right, one real disparity
+//            per lane, and keeps the running sum of the last blockSize
+//            costs (sums along x, into shared memory);
+//   phase 2: a thread per pixel adds blockSize rows of those sums, two
+//            labels per 32-bit add, from its own real-disparity offset.
+// Window sums are exact integers (at most 25 * 255 here, no intermediate
+// clamp in the reference).  Tiles whose parents disagree more widely, or a
+// wider window, evaluate each window directly.
 // ---------------------------------------------------------------------------
-template <int NJ>
-__global__ void __launch_bounds__(256) k_cost_bt_local(const __grid_constant__ Jobs<NJ> jobs)
-{
-    const LevelDesc& J = jobs.d[blockIdx.y];
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)J.w * J.h * J.D;
-    if (i >= total) return;
-    const int d = (int)(i % J.D);
-    const long long p = i / J.D;
-    const int y = (int)(p / J.w), x = (int)(p - (long long)y * J.w);
-    const int base = J.base[p];
-    int lo, hi;
-    label_range(J, x, base, lo, hi);
-    int out = kMax;
-    if (d >= lo && d <= hi) {
-        const int real = base + d, half = J.bs / 2, W = J.w, H = J.h;
-        int sum = 0;
-        for (int dy = -half; dy <= half; ++dy) {
-            const int yy = iclamp(y + dy, 0, H - 1);
-            const uint2* lrow = J.featL + (size_t)yy * W;
-            const uint2* rrow = J.featR + (size_t)yy * W;
-            for (int dx = -half; dx <= half; ++dx) {
-                const int xx = iclamp(x + dx, 0, W - 1);
-                const int x2 = xx - real;
-                sum += (x2 >= 0 && x2 < W) ? bt_pixel(__ldg(&lrow[xx]), __ldg(&rrow[x2])) : 255;
-            }
-        }
-        out = imin(sum, kMax - 1);
-    }
-    J.C[i] = (int16_t)out;
-}
+constexpr int kTiX = 32, kTiY = 8, kTiRn = 64, kTiMaxHalf = 2;
+constexpr int kTiRs = kTiRn + 2;   // halves per (row, column): 33 words, odd, so columns hit distinct banks
+constexpr size_t kTiSmem = (size_t)(kTiY + 2 * kTiMaxHalf) * kTiX * kTiRs * 2;
 
-// ---------------------------------------------------------------------------
-// BT refine cost, tiled.  Same values as k_cost_bt_local, computed per
-// 32x8 tile from the BT costs of every (window pixel, real disparity) pair
-// the tile needs: the real disparities of a tile are
-// [min base, max base + D - 1]; when that span is at most kTiRn, the BT
-// cost of each (clamped window pixel, real disparity) is evaluated once into
-// shared memory, summed along x, then along y, and each voxel picks the sum
-// at its own real disparity.  Window sums are exact integers (no
-// intermediate clamp in the reference) and clamped to kMax - 1 at the end.
-// Tiles whose parents disagree more widely fall back to direct evaluation.
-// ---------------------------------------------------------------------------
-constexpr int kTiX = 32, kTiY = 8, kTiRn = 32, kTiMaxHalf = 2;
+// Sums along x of one window row r (image row gy) for the 32 real
+// disparities rmin + r0 + lane: a running sum over the last 2*HW+1 costs.
+template <int HW>
+__device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, int r, int gy, int x0, int rmin,
+                                            int r0, int rn, int lane)
+{
+    const int W = J.w;
+    const uint2* lrow = J.featL + (size_t)gy * W;
+    const uint2* rrow = J.featR + (size_t)gy * W;
+    const int ri = r0 + lane;
+    const int real = rmin + ri;
+    int q[2 * HW + 1];   // q[0 .. 2HW-1]: the last 2HW costs, oldest first
+#pragma unroll
+    for (int i = 0; i < 2 * HW + 1; ++i) q[i] = 0;
+    int s = 0;
+    for (int j = 0; j < kTiX + 2 * HW; ++j) {
+        const int gx = iclamp(x0 - HW + j, 0, W - 1);
+        const int x2 = gx - real;
+        const int e = (x2 >= 0 && x2 < W) ? bt_pixel(__ldg(&lrow[gx]), __ldg(&rrow[x2])) : 255;
+        s += e;
+        if (j >= 2 * HW && ri < rn) hs[(r * kTiX + j - 2 * HW) * kTiRs + ri] = (uint16_t)s;
+        if (HW > 0) {
+            s -= q[0];
+#pragma unroll
+            for (int i = 0; i + 1 < 2 * HW; ++i) q[i] = q[i + 1];
+            q[2 * HW - 1 < 0 ? 0 : 2 * HW - 1] = e;
+        } else {
+            s = 0;
+        }
+    }
+}
 
 template <int NJ>
 __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ Jobs<NJ> jobs)
@@ -354,96 +365,100 @@ __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ J
     const int x0 = blockIdx.x * kTiX, y0 = blockIdx.y * kTiY;
     if (x0 >= J.w || y0 >= J.h) return;
     const int W = J.w, H = J.h, D = J.D, h = J.bs / 2;
-    constexpr int SW = kTiX + 2 * kTiMaxHalf, SH = kTiY + 2 * kTiMaxHalf;
-    __shared__ uint8_t bt[SH][SW][kTiRn];            // BT cost per (row, col, r - rmin)
-    __shared__ uint16_t hs[SH][kTiX][kTiRn];         // sums along x
-    __shared__ int16_t sbase[kTiY][kTiX];
-    __shared__ int red[2];
-    const int tid = threadIdx.x;
-    const int tx = tid & (kTiX - 1), ty = tid / kTiX;
-    const int x = x0 + tx, y = y0 + ty;
+    extern __shared__ __align__(16) uint16_t hs[];   // [kTiY + 2h][kTiX][kTiRs]
+    __shared__ int wred[2][kTiY];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x = x0 + lane, y = y0 + warp;
     const bool inside = x < W && y < H;
-    int b = kNoParent;
-    if (inside) b = J.base[(size_t)y * W + x];
-    sbase[ty][tx] = (int16_t)b;
-    if (tid == 0) { red[0] = INT_MAX; red[1] = INT_MIN; }
+    const int b = inside ? (int)J.base[(size_t)y * W + x] : (int)kNoParent;
+    const bool has = inside && b != kNoParent;
+    const int bmin = __reduce_min_sync(0xffffffffu, has ? b : INT_MAX);
+    const int bmax = __reduce_max_sync(0xffffffffu, has ? b : INT_MIN);
+    if (lane == 0) { wred[0][warp] = bmin; wred[1][warp] = bmax; }
     __syncthreads();
-    if (inside && b != kNoParent) {
-        atomicMin(&red[0], b);
-        atomicMax(&red[1], b);
-    }
-    __syncthreads();
-    const int rmin = red[0], rmax = red[1] + D - 1;
-    const bool tiled = red[1] != INT_MIN && rmax - rmin + 1 <= kTiRn && h <= kTiMaxHalf;
+    int rmin = INT_MAX, rmax = INT_MIN;
+#pragma unroll
+    for (int i = 0; i < kTiY; ++i) { rmin = imin(rmin, wred[0][i]); rmax = imax(rmax, wred[1][i]); }
+    const bool any = rmax != INT_MIN;
+    rmax += D - 1;
+    const bool tiled = any && rmax - rmin + 1 <= kTiRn && h <= kTiMaxHalf;
     if (tiled) {
         const int rn = rmax - rmin + 1;
-        const int sw = kTiX + 2 * h, sh = kTiY + 2 * h;
-        for (int i = tid; i < sh * sw * rn; i += blockDim.x) {
-            const int ri = i % rn;
-            const int j = (i / rn) % sw;
-            const int r = i / (rn * sw);
-            const int gy = iclamp(y0 - h + r, 0, H - 1), gx = iclamp(x0 - h + j, 0, W - 1);
-            const int x2 = gx - (rmin + ri);
-            int v = 255;
-            if (x2 >= 0 && x2 < W) v = bt_pixel(J.featL[(size_t)gy * W + gx], J.featR[(size_t)gy * W + x2]);
-            bt[r][j][ri] = (uint8_t)v;
+        const int nch = (rn + 31) >> 5;   // 32 real disparities per warp pass
+        for (int u = warp; u < (kTiY + 2 * h) * nch; u += kTiY) {
+            const int r = u / nch, r0 = (u - r * nch) * 32;
+            const int gy = iclamp(y0 - h + r, 0, H - 1);
+            if (h == 2) bt_row_sums<2>(J, hs, r, gy, x0, rmin, r0, rn, lane);
+            else if (h == 1) bt_row_sums<1>(J, hs, r, gy, x0, rmin, r0, rn, lane);
+            else bt_row_sums<0>(J, hs, r, gy, x0, rmin, r0, rn, lane);
         }
-        __syncthreads();
-        for (int i = tid; i < sh * kTiX * rn; i += blockDim.x) {
-            const int ri = i % rn;
-            const int j = (i / rn) % kTiX;
-            const int r = i / (rn * kTiX);
-            int s = 0;
-            for (int k = 0; k <= 2 * h; ++k) s += bt[r][j + k][ri];
-            hs[r][j][ri] = (uint16_t)s;
-        }
-        __syncthreads();
-        // one (pixel, label) per thread and pass: consecutive threads write consecutive labels
-        for (int i = tid; i < kTiX * kTiY * D; i += blockDim.x) {
-            const int d = i % D;
-            const int px = (i / D) % kTiX;
-            const int py = i / (D * kTiX);
-            const int xx = x0 + px, yy = y0 + py;
-            if (xx >= W || yy >= H) continue;
-            const int base = sbase[py][px];
-            int lo, hi;
-            label_range(J, xx, base, lo, hi);
-            int out = kMax;
-            if (d >= lo && d <= hi) {
-                const int ri = base + d - rmin;
-                int s = 0;
-                for (int k = 0; k <= 2 * h; ++k) s += hs[py + k][px][ri];
-                out = imin(s, kMax - 1);
+    }
+    __syncthreads();
+    if (!inside) return;
+    int lo, hi;
+    label_range(J, x, b, lo, hi);
+    int16_t* out = J.C + ((size_t)y * W + x) * D;
+    const bool vec = (D & 7) == 0;
+    if (tiled && b != kNoParent) {
+        // packed pair sums of 2h+1 rows from offset ri0 = b - rmin (halves), 8 labels per chunk
+        const int ri0 = b - rmin;
+        const uint32_t sh = (uint32_t)(ri0 & 1) * 16;
+        for (int d0 = 0; d0 < D; d0 += 8) {
+            uint32_t acc[5] = {0u, 0u, 0u, 0u, 0u};
+            for (int k = 0; k <= 2 * h; ++k) {
+                const uint32_t* row =
+                    reinterpret_cast<const uint32_t*>(hs + ((warp + k) * kTiX + lane) * kTiRs) + ((ri0 + d0) >> 1);
+#pragma unroll
+                for (int j = 0; j < 5; ++j) acc[j] += row[j];
             }
-            J.C[((size_t)yy * W + xx) * D + d] = (int16_t)out;
+            uint32_t w[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                w[i] = __funnelshift_r(acc[i], acc[i + 1], sh);
+                const int d = d0 + 2 * i;
+                if (d < lo || d > hi) w[i] = (w[i] & 0xffff0000u) | (uint32_t)kMax;
+                if (d + 1 < lo || d + 1 > hi) w[i] = (w[i] & 0xffffu) | ((uint32_t)kMax << 16);
+            }
+            if (vec) {
+                reinterpret_cast<uint4*>(out + d0)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+            } else {
+                for (int i = 0; i < 8 && d0 + i < D; ++i)
+                    out[d0 + i] = (int16_t)((w[i >> 1] >> ((i & 1) * 16)) & 0xffffu);
+            }
         }
-    } else {
-        for (int i = tid; i < kTiX * kTiY * D; i += blockDim.x) {
-            const int d = i % D;
-            const int px = (i / D) % kTiX;
-            const int py = i / (D * kTiX);
-            const int xx = x0 + px, yy = y0 + py;
-            if (xx >= W || yy >= H) continue;
-            const int base = sbase[py][px];
-            int lo, hi;
-            label_range(J, xx, base, lo, hi);
-            int out = kMax;
-            if (d >= lo && d <= hi) {
-                const int real = base + d;
-                int sum = 0;
-                for (int dy = -h; dy <= h; ++dy) {
-                    const int gy = iclamp(yy + dy, 0, H - 1);
-                    const uint2* lrow = J.featL + (size_t)gy * W;
-                    const uint2* rrow = J.featR + (size_t)gy * W;
-                    for (int dx = -h; dx <= h; ++dx) {
-                        const int gx = iclamp(xx + dx, 0, W - 1);
-                        const int x2 = gx - real;
-                        sum += (x2 >= 0 && x2 < W) ? bt_pixel(__ldg(&lrow[gx]), __ldg(&rrow[x2])) : 255;
+        return;
+    }
+    // direct window per pixel
+    for (int d0 = 0; d0 < D; d0 += 8) {
+        int sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (b != kNoParent) {
+            for (int dy = -h; dy <= h; ++dy) {
+                const int gy = iclamp(y + dy, 0, H - 1);
+                const uint2* lrow = J.featL + (size_t)gy * W;
+                const uint2* rrow = J.featR + (size_t)gy * W;
+                for (int dx = -h; dx <= h; ++dx) {
+                    const int gx = iclamp(x + dx, 0, W - 1);
+                    const uint2 lf = __ldg(&lrow[gx]);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int x2 = gx - (b + d0 + i);
+                        sum[i] += (x2 >= 0 && x2 < W) ? bt_pixel(lf, __ldg(&rrow[x2])) : 255;
                     }
                 }
-                out = imin(sum, kMax - 1);
             }
-            J.C[((size_t)yy * W + xx) * D + d] = (int16_t)out;
+        }
+        uint32_t w[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int d = d0 + 2 * i;
+            const uint32_t v0 = (d >= lo && d <= hi) ? (uint32_t)imin(sum[2 * i], kMax - 1) : (uint32_t)kMax;
+            const uint32_t v1 = (d + 1 >= lo && d + 1 <= hi) ? (uint32_t)imin(sum[2 * i + 1], kMax - 1) : (uint32_t)kMax;
+            w[i] = v0 | (v1 << 16);
+        }
+        if (vec) {
+            reinterpret_cast<uint4*>(out + d0)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        } else {
+            for (int i = 0; i < 8 && d0 + i < D; ++i) out[d0 + i] = (int16_t)((w[i >> 1] >> ((i & 1) * 16)) & 0xffffu);
         }
     }
 }
@@ -506,12 +521,14 @@ cudaError_t launch_cost(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t
     const LevelDesc& J0 = jobs.d[0];
     prof_begin(st);
     if (J0.cost == COST_CENSUS) {
-        const long long n = e.max_vox / 2;
-        dim3 g((unsigned)((n + 255) / 256), jobs.n);
+        dim3 g((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
         k_cost_census<NJ><<<g, 256, 0, st>>>(jobs);
     } else if (J0.refine) {
+        cudaError_t err = cudaFuncSetAttribute(k_cost_bt_tiled<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kTiSmem);
+        if (err != cudaSuccess) return err;
         dim3 g((e.max_w + kTiX - 1) / kTiX, (e.max_h + kTiY - 1) / kTiY, jobs.n);
-        k_cost_bt_tiled<NJ><<<g, 256, 0, st>>>(jobs);
+        k_cost_bt_tiled<NJ><<<g, 256, kTiSmem, st>>>(jobs);
     } else {
         int maxHalf = 0;
         for (int j = 0; j < jobs.n; ++j) maxHalf = std::max(maxHalf, jobs.d[j].bs / 2);

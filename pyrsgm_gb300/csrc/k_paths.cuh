@@ -759,9 +759,9 @@ template <bool PYR, int NJ>
 cudaError_t launch_paths_mode(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
     switch (path_variant(jobs.d[0].D)) {
-    case 10016: return launch_paths_packed<2, PYR, NJ>(jobs, e, st);
-    case 10032: return launch_paths_packed<4, PYR, NJ>(jobs, e, st);
-    case 10064: return launch_paths_packed<8, PYR, NJ>(jobs, e, st);
+    case 10016: return launch_paths_packed<1, PYR, NJ>(jobs, e, st);
+    case 10032: return launch_paths_packed<2, PYR, NJ>(jobs, e, st);
+    case 10064: return launch_paths_packed<4, PYR, NJ>(jobs, e, st);
     case 1601: return launch_paths_shape<16, 1, PYR, NJ>(jobs, e, st);
     case 3201: return launch_paths_shape<32, 1, PYR, NJ>(jobs, e, st);
     case 3202: return launch_paths_shape<32, 2, PYR, NJ>(jobs, e, st);

@@ -1,6 +1,7 @@
-// k_paths_packed.cuh -- path aggregation for D = 8*T labels (16, 32, 64):
-// the labels of one path chain are packed two per 32-bit word and spread
-// over a group of T adjacent threads, four words (eight labels) each.
+// k_paths_packed.cuh -- path aggregation for D = 16*T labels (16, 32, 64):
+// the labels of one path chain are packed two per 32-bit word and held by
+// T threads, eight words (sixteen labels) each; T = 1 for the 16-label
+// refine levels, so a chain is one thread.
 //
 // The recurrence of a step (reference: src/sgm_kernels.cu:560-565
 // single-scale, 1230-1252 pyramid) runs on 16-bit pairs with the DPX
@@ -22,19 +23,25 @@
 //   * an active chain whose best is SHRT_MAX gives SHRT_MAX (the sign of
 //     best + 1 per half, replicated by prmt).
 //
-// Each step a thread stores its four words of the previous step into a
-// guard-padded shared buffer of its chain (double-buffered, one __syncwarp
-// per step) and reads back the six words of its shifted window; chain
-// minima and WTA argmins reduce over the group by __shfl_xor_sync.  The
-// buffers are placed so that the 32 threads of a warp touch 32 different
-// banks whenever the chains share their label shift.
+// Shifted windows: each step a thread stores its eight words of the
+// previous step into its chain's guard-padded shared buffer and reads back
+// the ten words of its shifted window (word w of chain c at w * CPW + c, so
+// a one-thread chain touches only its own bank).  Chains of T > 1 threads
+// double-buffer the window and exchange it with one __syncwarp per step;
+// their minima and argmins reduce by __shfl_xor_sync.
 //
-// Horizontal pass: a warp holds 16/T rows, each with an L->R group and an
-// R->L group walking towards each other; the first chain at a pixel leaves
-// its partial sum (with the top->bottom costs) in V, or in a shared-memory
-// band near the meeting point, the second finishes the pixel (deferred WTA).
-// The disp2 candidates go to the per-pixel keys with atomicMin; the LR check
-// reads them in the post kernel.
+// Loads: per thread a ring of kStages steps in shared memory filled with
+// cp.async (costs, partial sums, label base, image byte), so the loads of
+// a step are issued kStages - 1 steps before it without holding registers.
+//
+// Horizontal pass: a warp holds 16/T rows, each with an L->R chain group
+// and an R->L chain group walking towards each other.  The first chain at a
+// pixel leaves its partial sum (with the top->bottom costs) in V; the
+// second reads it back (from the ring, or with a plain load after the
+// per-step __syncwarp when the first wrote it less than kStages + 2 steps
+// earlier), adds its own costs and picks the winner.  The pixel both reach
+// at the same step is finished after the walk.  disp2 candidates go to the
+// per-pixel keys with atomicMin; the LR check reads them in the post kernel.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -50,8 +57,11 @@ namespace pk {
 
 constexpr uint32_t kMax2 = 0x7fff7fffu;
 constexpr uint32_t kOne2 = 0x00010001u;
-constexpr int kPF = 4;      // register prefetch distance in steps
-constexpr int kWarps = 4;   // warps per block
+constexpr int kWarps = 4;        // warps per block
+constexpr int kStages = 6;       // look-ahead of the horizontal pass (steps)
+constexpr int kStagesTb = 8;     // look-ahead of the top->bottom pass
+constexpr int kRowRsw = 20;      // ring words per thread and stage: c[8] v[8] base img (+2: conflict-free 16-B lanes)
+constexpr int kTbRsw = 12;       // c[8] base img (+2)
 
 __device__ __forceinline__ uint32_t dup(int v) { return ((uint32_t)v & 0xffffu) * 0x10001u; }
 
@@ -63,65 +73,80 @@ __device__ __forceinline__ uint32_t sign_mask2(uint32_t x)
     return r;
 }
 
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void cp16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp4(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// The aligned 32-bit word holding the byte at p (it lies in the same
+// allocation as the byte).
+__device__ __forceinline__ const void* word_of(const void* p)
+{
+    return reinterpret_cast<const void*>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)3);
+}
+__device__ __forceinline__ int byte_shift(const void* p) { return (int)(reinterpret_cast<uintptr_t>(p) & 3) * 8; }
+
 template <int T>
 struct Grp {
-    static constexpr int D = 8 * T;             // labels per chain
+    static constexpr int D = 16 * T;            // labels per chain
     static constexpr int CPW = 32 / T;          // chains per warp
     static constexpr int PADW = D / 2 + 1;      // guard words before label 0 (D + 2 halves)
     static constexpr int LENW = PADW + D + 2;   // words a shifted window can touch
-    static constexpr int GPB = 8 / T;           // chains per 32-bank row of the layout
-    static constexpr int NEED = LENW + 35 - 4 * T;
-    static constexpr int CS = (NEED + 31) / 32 * 32;   // chain stride (words, multiple of 32)
-    static constexpr int BUFW = CPW * CS;              // one buffer of a warp
-    // Word offset of chain c's buffer: c * CS plus a bank offset so that
-    // word j of thread k of chain c lands in bank off(c) + 4k + j (mod 32),
-    // distinct over the warp.
-    __device__ static int off(int c) { return c * CS + 4 * T * (c % GPB) + c / GPB; }
+    static constexpr int BUFW = LENW * CPW;     // one window buffer of a warp
+    static constexpr int NBUF = T == 1 ? 1 : 2;
 };
 
-template <int T>
 struct GChain {
-    uint32_t L[4];
+    uint32_t L[8];
     int mp;        // minimum of the previous step over the chain's labels
     int prevBase;
 };
 
-template <int T>
-__device__ __forceinline__ void gchain_init(GChain<T>& s, int minD)
+__device__ __forceinline__ void gchain_init(GChain& s, int minD)
 {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) s.L[i] = kMax2;
+    for (int i = 0; i < 8; ++i) s.L[i] = kMax2;
     s.mp = 0x7fff;
     s.prevBase = minD;
 }
 
-// One step of the chain: c = this thread's eight costs of the pixel,
-// buf = the chain's buffer of this step's parity.
+// One step of the chain: c = this thread's sixteen costs of the pixel,
+// buf = word 0 of the chain's window buffer (this step's parity).
 template <int T, bool PYR>
-__device__ __forceinline__ void gstep(GChain<T>& s, const uint32_t (&c)[4], int base, int p2, uint32_t p12,
+__device__ __forceinline__ void gstep(GChain& s, const uint32_t (&c)[8], int base, int p2, uint32_t p12,
                                       uint32_t* buf, int k)
 {
     using G = Grp<T>;
-    constexpr int D = G::D;
+    constexpr int D = G::D, ST = G::CPW;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) buf[G::PADW + 4 * k + i] = s.L[i];
-    __syncwarp();
+    for (int i = 0; i < 8; ++i) buf[(G::PADW + 8 * k + i) * ST] = s.L[i];
+    if (T > 1) __syncwarp();
     int delta = PYR ? base - s.prevBase : 0;
     delta = iclamp(delta, -(D + 1), D + 1);
-    const int i0 = 2 * G::PADW + delta - 1 + 8 * k;    // half index of label (8k - 1) after the shift
-    const uint32_t* wp = buf + (i0 >> 1);
+    const int i0 = 2 * G::PADW + delta - 1 + 16 * k;   // half index of label (16k - 1) after the shift
+    const uint32_t* wp = buf + (i0 >> 1) * ST;
     const uint32_t sh = (uint32_t)(i0 & 1) * 16;
-    uint32_t w0[6];
+    uint32_t w0[10];
 #pragma unroll
-    for (int j = 0; j < 6; ++j) w0[j] = wp[j];
-    uint32_t w[5];
+    for (int j = 0; j < 10; ++j) w0[j] = wp[j * ST];
+    uint32_t w[9];
 #pragma unroll
-    for (int j = 0; j < 5; ++j) w[j] = __funnelshift_r(w0[j], w0[j + 1], sh);
+    for (int j = 0; j < 9; ++j) w[j] = __funnelshift_r(w0[j], w0[j + 1], sh);
     const int lj = imin(0x7fff, s.mp + p2);
     const uint32_t lj2 = dup(lj), mp2 = dup(s.mp);
     const uint32_t inc2 = (PYR && s.mp < 0x7fff) ? kOne2 : 0u;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < 8; ++m) {
         const uint32_t n0 = __funnelshift_r(w[m], w[m + 1], 16);   // (L[s], L[s+1])
         const uint32_t t = __viaddmin_u16x2(w[m], p12, lj2);       // min(L[s-1] + P1, lj)
         const uint32_t best = __vimin3_u16x2(n0, t, w[m + 1] + p12);
@@ -129,7 +154,8 @@ __device__ __forceinline__ void gstep(GChain<T>& s, const uint32_t (&c)[4], int 
         if constexpr (PYR) v |= sign_mask2(best + inc2) & kMax2;
         s.L[m] = v;
     }
-    uint32_t m2 = __vminu2(__vimin3_u16x2(s.L[0], s.L[1], s.L[2]), s.L[3]);
+    uint32_t m2 = __vminu2(__vimin3_u16x2(s.L[0], s.L[1], s.L[2]), __vimin3_u16x2(s.L[3], s.L[4], s.L[5]));
+    m2 = __vimin3_u16x2(m2, s.L[6], s.L[7]);
 #pragma unroll
     for (int o = 1; o < T; o <<= 1) m2 = __vminu2(m2, __shfl_xor_sync(0xffffffffu, m2, o));
     s.mp = imin((int)(m2 & 0xffffu), (int)(m2 >> 16));
@@ -137,13 +163,12 @@ __device__ __forceinline__ void gstep(GChain<T>& s, const uint32_t (&c)[4], int 
 }
 
 // Coarse pyramid levels: labels outside label_range take SHRT_MAX.
-template <int T>
-__device__ __forceinline__ void mask_labels(uint32_t (&c)[4], int lo, int hi, int k)
+__device__ __forceinline__ void mask_labels(uint32_t (&c)[8], int lo, int hi, int k)
 {
-    if (lo <= 8 * k && hi >= 8 * k + 7) return;
+    if (lo <= 16 * k && hi >= 16 * k + 15) return;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int d0 = 8 * k + 2 * i;
+    for (int i = 0; i < 8; ++i) {
+        const int d0 = 16 * k + 2 * i;
         const bool ok0 = d0 >= lo && d0 <= hi, ok1 = d0 + 1 >= lo && d0 + 1 <= hi;
         c[i] |= (ok0 ? 0u : 0x7fffu) | (ok1 ? 0u : 0x7fff0000u);
     }
@@ -162,57 +187,25 @@ __device__ __forceinline__ uint32_t gcombine(uint32_t a, uint32_t b)
     }
 }
 
-__device__ __forceinline__ void to4(const uint4 q, uint32_t (&v)[4])
+__device__ __forceinline__ void ld8(const uint32_t* p, uint32_t (&v)[8])
 {
-    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    const uint4 a = reinterpret_cast<const uint4*>(p)[0], b = reinterpret_cast<const uint4*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
-__device__ __forceinline__ uint4 from4(const uint32_t (&v)[4]) { return make_uint4(v[0], v[1], v[2], v[3]); }
-
-// Winner-take-all of one pixel over a chain group (kernel_WTA_Subpixel,
-// src/sgm_kernels.cu:573-640; pyramid kernel_PyramidWTA,
-// src/sgm_kernels.cu:1290-1370).  Every lane of the warp calls it; `doit`
-// gates the writes.  scr: this warp's 128-word scratch.
-template <int T, bool PYR>
-__device__ __forceinline__ void gwta(const LevelDesc& J, bool doit, int y, int x, const uint32_t (&tot)[4], int base,
-                                     uint32_t* scr, int lane, int k)
+__device__ __forceinline__ void st8(uint32_t* p, const uint32_t (&v)[8])
 {
-    constexpr int D = 8 * T;
-    // first label of the minimum: per thread, then over the group (cost << 16 | label)
-    const uint32_t m2 = __vminu2(__vimin3_u16x2(tot[0], tot[1], tot[2]), tot[3]);
-    const int lmin = imin((int)(m2 & 0xffffu), (int)(m2 >> 16));
-    const uint32_t mc2 = dup(lmin);
-    int li = 7;
-#pragma unroll
-    for (int i = 3; i >= 0; --i) {
-        const uint32_t e = tot[i] - mc2;                       // zero half where equal (no borrow)
-        const uint32_t z = (e - kOne2) & ~e & 0x80008000u;     // lowest set bit marks the first zero half
-        if (z) li = 2 * i + ((z & 0x8000u) ? 0 : 1);
-    }
-    unsigned key = ((unsigned)lmin << 16) | (unsigned)(8 * k + li);
-#pragma unroll
-    for (int o = 1; o < T; o <<= 1) key = umin(key, __shfl_xor_sync(0xffffffffu, key, o));
-    const int minCost = (int)(key >> 16), bestD = (int)(key & 0xffffu);
-    // neighbours of the best label, then the minimum over |d - best| > 1
-    reinterpret_cast<uint4*>(scr)[lane] = from4(tot);
-    __syncwarp();
-    int16_t* lab = reinterpret_cast<int16_t*>(scr) + (lane - k) * 8;
-    const bool owner = (bestD >> 3) == k;
-    int c0 = 0, c1 = 0, c2 = 0;
-    if (owner) {
-        c1 = lab[bestD];
-        if (bestD > 0) { c0 = lab[bestD - 1]; lab[bestD - 1] = 0x7fff; }
-        if (bestD + 1 < D) { c2 = lab[bestD + 1]; lab[bestD + 1] = 0x7fff; }
-        lab[bestD] = 0x7fff;
-    }
-    __syncwarp();
-    uint32_t q[4];
-    to4(reinterpret_cast<const uint4*>(scr)[lane], q);
-    const uint32_t a2 = __vminu2(__vimin3_u16x2(q[0], q[1], q[2]), q[3]);
-    int alt = imin((int)(a2 & 0xffffu), (int)(a2 >> 16));
-#pragma unroll
-    for (int o = 1; o < T; o <<= 1) alt = imin(alt, __shfl_xor_sync(0xffffffffu, alt, o));
-    __syncwarp();   // the scratch is rewritten by the next call
-    if (!(owner && doit)) return;
+    reinterpret_cast<uint4*>(p)[0] = make_uint4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<uint4*>(p)[1] = make_uint4(v[4], v[5], v[6], v[7]);
+}
+
+// Outputs of a winner (kernel_WTA_Subpixel, src/sgm_kernels.cu:573-640;
+// pyramid kernel_PyramidWTA, src/sgm_kernels.cu:1290-1370): minimum cost,
+// first label reaching it, the minimum over labels farther than one from
+// it, and the costs next to it (c0, c2; 0 outside the range).
+template <int D, bool PYR>
+__device__ __forceinline__ void wta_out(const LevelDesc& J, int y, int x, int base, int minCost, int bestD, int alt,
+                                        int c0, int c1, int c2)
+{
     const int16_t inv = (int16_t)((J.minD - 1) * 16);
     int16_t dout = inv;
     float cout = 0.0f;
@@ -265,23 +258,17 @@ __device__ __forceinline__ void gwta(const LevelDesc& J, bool doit, int y, int x
     J.conf_raw[p] = cout;
 }
 
-// Inputs of one pixel, loaded kPF steps ahead.
-struct GPre {
-    uint4 c;
-    uint4 v;
-    int base;
-    int img;
-};
-
-template <bool PYR>
-__device__ __forceinline__ void gprefetch(const LevelDesc& J, int y, int x, int k, int D, bool need_v, GPre& f)
+template <int T>
+constexpr size_t row_smem()
 {
-    const size_t p = (size_t)y * J.w + x;
-    const size_t o = p * D + 8 * k;
-    f.c = __ldg(reinterpret_cast<const uint4*>(J.C + o));
-    if (need_v) f.v = *reinterpret_cast<const uint4*>(J.V + o);   // may hold this kernel's own partials
-    f.base = (PYR && J.refine) ? (int)__ldg(J.base + p) : J.minD;
-    f.img = J.adaptive ? (int)__ldg(J.left + (size_t)y * J.lstep + x) : 0;
+    using G = Grp<T>;
+    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStages * 32 * kRowRsw + (G::CPW / 2) * (G::D / 2));
+}
+template <int T>
+constexpr size_t tb_smem()
+{
+    using G = Grp<T>;
+    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStagesTb * 32 * kTbRsw);
 }
 
 }  // namespace pk
@@ -294,12 +281,14 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
 {
     using namespace pk;
     using G = Grp<T>;
-    constexpr int D = G::D;
+    constexpr int D = G::D, S = kStagesTb;
     const LevelDesc& J = jobs.d[blockIdx.y];
-    __shared__ int lut[256];
-    __shared__ __align__(16) uint32_t cbuf[kWarps * 2 * G::BUFW];
+    extern __shared__ __align__(16) uint32_t smem[];
+    int* lut = reinterpret_cast<int*>(smem);
+    uint32_t* cbuf = smem + 256;
+    uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
-    for (int i = threadIdx.x; i < kWarps * 2 * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
+    for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = lane / T, k = lane % T;
@@ -310,35 +299,52 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
     if (col0 >= ncol) return;   // the whole warp is past the image
     const int col = col0 + c;
     const bool col_ok = col < ncol;
-    const int x = xlo + imin(col, ncol - 1), H = J.h;
-    uint32_t* bufs = cbuf + warp * 2 * G::BUFW + G::off(c);
+    const int x = xlo + imin(col, ncol - 1), H = J.h, W = J.w;
+    uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
+    uint32_t* ring = rbuf + (warp * S * 32 + lane) * kTbRsw;
     const uint32_t p12 = dup(imin(J.P1, 0x8000));
     int lo = 0, hi = D - 1;
     if (PYR && !J.refine) label_range(J, x, J.minD, lo, hi);
-    GChain<T> s;
+    const bool use_base = PYR && J.refine, adaptive = J.adaptive != 0;
+    const int16_t* cp = J.C + (size_t)x * D + 16 * k;
+    const size_t cstep = (size_t)W * D;
+    auto issue = [&](int y, int slot) {
+        uint32_t* d = ring + slot * 32 * kTbRsw;
+        const int16_t* src = cp + (size_t)y * cstep;
+        cp16(d, src);
+        cp16(d + 4, src + 8);
+        if (use_base) cp4(d + 8, word_of(J.base + (size_t)y * W + x));
+        if (adaptive) cp4(d + 9, word_of(J.left + (size_t)y * J.lstep + x));
+    };
+    GChain s;
     gchain_init(s, J.minD);
-    GPre ring[kPF] = {};
 #pragma unroll
-    for (int j = 0; j < kPF; ++j)
-        if (j < H) gprefetch<PYR>(J, j, x, k, D, false, ring[j]);
-    int img_prev = 0;
-    for (int y0 = 0; y0 < H; y0 += kPF) {
-#pragma unroll
-        for (int j = 0; j < kPF; ++j) {
-            const int y = y0 + j;
-            if (y >= H) break;
-            const GPre cur = ring[j];
-            if (y + kPF < H) gprefetch<PYR>(J, y + kPF, x, k, D, false, ring[j]);
-            const int p2 = J.adaptive ? lut[abs(cur.img - img_prev) & 255] : J.P2;
-            img_prev = cur.img;
-            uint32_t cc[4];
-            to4(cur.c, cc);
-            if (PYR && !J.refine) mask_labels<T>(cc, lo, hi, k);
-            gstep<T, PYR>(s, cc, cur.base, p2, p12, bufs + (y & 1) * G::BUFW, k);
-            if (col_ok)
-                *reinterpret_cast<uint4*>(J.V + ((size_t)y * J.w + x) * D + 8 * k) = from4(s.L);
-        }
+    for (int j = 0; j < S - 1; ++j) {
+        if (j < H) issue(j, j);
+        cp_commit();
     }
+    int img_prev = 0, slot = 0, islot = S - 1;
+    for (int y = 0; y < H; ++y) {
+        if (y + S - 1 < H) issue(y + S - 1, islot);
+        cp_commit();
+        islot = islot + 1 == S ? 0 : islot + 1;
+        cp_wait<S - 1>();
+        const uint32_t* d = ring + slot * 32 * kTbRsw;
+        slot = slot + 1 == S ? 0 : slot + 1;
+        uint32_t cc[8];
+        ld8(d, cc);
+        const int base = use_base ? (int)(int16_t)(d[8] >> ((((size_t)y * W + x) & 1) * 16)) : J.minD;
+        int p2 = J.P2;
+        if (adaptive) {
+            const int img = (int)((d[9] >> byte_shift(J.left + (size_t)y * J.lstep + x)) & 255u);
+            p2 = lut[abs(img - img_prev) & 255];
+            img_prev = img;
+        }
+        if (PYR && !J.refine) mask_labels(cc, lo, hi, k);
+        gstep<T, PYR>(s, cc, base, p2, p12, chain + (G::NBUF == 2 ? (y & 1) * G::BUFW : 0), k);
+        if (col_ok) st8(reinterpret_cast<uint32_t*>(J.V + (size_t)y * cstep + (size_t)x * D + 16 * k), s.L);
+    }
+    cp_wait<0>();
 }
 
 // ---------------------------------------------------------------------------
@@ -350,15 +356,15 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
 {
     using namespace pk;
     using G = Grp<T>;
-    constexpr int D = G::D, DW = D / 2, RPW = G::CPW / 2, NB = kPF + 3;
+    constexpr int D = G::D, RPW = G::CPW / 2, S = kStages;
     const LevelDesc& J = jobs.d[blockIdx.y];
-    __shared__ int lut[256];
-    __shared__ __align__(16) uint32_t cbuf[kWarps * 2 * G::BUFW];
-    __shared__ __align__(16) uint32_t scrb[kWarps * 128];
-    __shared__ __align__(16) uint32_t bandb[kWarps * RPW * NB * DW];
-    __shared__ __align__(16) uint32_t midb[kWarps * RPW * DW];
+    extern __shared__ __align__(16) uint32_t smem[];
+    int* lut = reinterpret_cast<int*>(smem);
+    uint32_t* cbuf = smem + 256;
+    uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
+    uint32_t* mbuf = rbuf + kWarps * S * 32 * kRowRsw;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
-    for (int i = threadIdx.x; i < kWarps * 2 * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
+    for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = lane / T, k = lane % T, r = c >> 1, dir = c & 1;
@@ -368,10 +374,9 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     const bool row_ok = y < J.h;
     const int yy = imin(y, J.h - 1);
     const int W = J.w;
-    uint32_t* bufs = cbuf + warp * 2 * G::BUFW + G::off(c);
-    uint32_t* band = bandb + (warp * RPW + r) * NB * DW;
-    uint32_t* mid = midb + (warp * RPW + r) * DW;
-    uint32_t* scr = scrb + warp * 128;
+    uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
+    uint32_t* ring = rbuf + (warp * S * 32 + lane) * kRowRsw;
+    uint32_t* mid = mbuf + (warp * RPW + r) * (D / 2);
 
     // path extents (single-scale: kernel_AggregateLR/RL ranges)
     int minX1 = 0, maxX1 = W, lr_x0 = 0, lr_n, rl_n;
@@ -388,12 +393,11 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     const bool has_lr = lr_n > 0, has_tb = J.paths >= 3;
     const int n_mine = dir == 0 ? lr_n : rl_n;
     const int Tn = imax(lr_n, rl_n);
-    const int C2 = W - 1 + lr_x0;                  // 2x at the meeting point
-    const int band_lo = (C2 - kPF - 1 + 1) >> 1;   // first x with |2x - C2| <= kPF + 1
-    auto in_band = [&](int x) { return abs(2 * x - C2) <= kPF + 1; };
+    const int C2 = W - 1 + lr_x0;   // 2x at the meeting point
+    // the first path left its partial less than S + 2 steps before: read it after the step's __syncwarp
+    auto late = [&](int x) { return abs(2 * x - C2) <= S + 1; };
     auto lr_covers = [&](int x) { return has_lr && x >= lr_x0 && x < lr_x0 + lr_n; };
     auto rl_covers = [&](int x) { return x >= W - rl_n; };
-    auto wta_px = [&](int x) { return PYR || (x >= minX1 && x < maxX1 && x != W - 1); };
     auto xpos = [&](int t) {
         return dir == 0 ? lr_x0 + imin(t, imax(lr_n - 1, 0)) : W - 1 - imin(t, imax(rl_n - 1, 0));
     };
@@ -406,98 +410,156 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
         const int tl = x - lr_x0;
         return tl < t ? 2 : (tl == t ? 4 : 1);
     };
-    auto need_v = [&](int ro, int x) { return (ro == 1 && has_tb) || (ro == 2 && !in_band(x)); };
-    auto prefetch = [&](int t, GPre& f) {
+    const bool use_base = PYR && J.refine, adaptive = J.adaptive != 0;
+    const size_t prow = (size_t)yy * W;
+    auto issue = [&](int t, int slot) {
         const int x = xpos(t);
-        gprefetch<PYR>(J, yy, x, k, D, need_v(role(t, x), x), f);
+        const int ro = role(t, x);
+        uint32_t* d = ring + slot * 32 * kRowRsw;
+        const size_t o = (prow + x) * D + 16 * k;
+        cp16(d, J.C + o);
+        cp16(d + 4, J.C + o + 8);
+        if ((ro == 1 && has_tb) || (ro == 2 && !late(x))) {
+            cp16(d + 8, J.V + o);
+            cp16(d + 12, J.V + o + 8);
+        }
+        if (use_base) cp4(d + 16, word_of(J.base + prow + x));
+        if (adaptive) cp4(d + 17, word_of(J.left + (size_t)yy * J.lstep + x));
     };
 
     const uint32_t p12 = dup(imin(J.P1, 0x8000));
-    GChain<T> s;
+    GChain s;
     gchain_init(s, J.minD);
-    GPre ring[kPF] = {};
 #pragma unroll
-    for (int j = 0; j < kPF; ++j)
-        if (j < n_mine) prefetch(j, ring[j]);
-    int img_prev = 0;
+    for (int j = 0; j < S - 1; ++j) {
+        if (j < n_mine) issue(j, j);
+        cp_commit();
+    }
+    int img_prev = 0, slot = 0, islot = S - 1;
     bool defer = false;
-    int xm = 0, base_m = 0;
-    for (int t0 = 0; t0 < Tn; t0 += kPF) {
+    int xm = 0;
+    for (int t = 0; t < Tn; ++t) {
+        if (t + S - 1 < n_mine) issue(t + S - 1, islot);
+        cp_commit();
+        islot = islot + 1 == S ? 0 : islot + 1;
+        cp_wait<S - 1>();
+        if (T == 1) __syncwarp();   // orders the other path's partial sums before the late reads below
+        const uint32_t* d = ring + slot * 32 * kRowRsw;
+        slot = slot + 1 == S ? 0 : slot + 1;
+        const int x = xpos(t);
+        uint32_t cc[8];
+        ld8(d, cc);
+        const int base = use_base ? (int)(int16_t)(d[16] >> (((prow + x) & 1) * 16)) : J.minD;
+        int p2 = J.P2;
+        if (adaptive) {
+            const int img = (int)((d[17] >> byte_shift(J.left + (size_t)yy * J.lstep + x)) & 255u);
+            p2 = lut[abs(img - img_prev) & 255];
+            img_prev = img;
+        }
+        if (PYR && !J.refine) {
+            int lo, hi;
+            label_range(J, x, J.minD, lo, hi);
+            mask_labels(cc, lo, hi, k);
+        }
+        uint32_t* cw = chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0);
+        gstep<T, PYR>(s, cc, base, p2, p12, cw, k);
+        const int ro = role(t, x);
+        uint32_t* vp = reinterpret_cast<uint32_t*>(J.V + (prow + x) * D + 16 * k);
+        if (ro == 1) {
+            uint32_t part[8];
+            if (has_tb) {
+                uint32_t vin[8];
+                ld8(d + 8, vin);
 #pragma unroll
-        for (int j = 0; j < kPF; ++j) {
-            const int t = t0 + j;
-            if (t >= Tn) break;
-            const int x = xpos(t);
-            const GPre cur = ring[j];
-            if (t + kPF < n_mine) prefetch(t + kPF, ring[j]);
-            const int p2 = J.adaptive ? lut[abs(cur.img - img_prev) & 255] : J.P2;
-            img_prev = cur.img;
-            uint32_t cc[4];
-            to4(cur.c, cc);
-            if (PYR && !J.refine) {
-                int lo, hi;
-                label_range(J, x, J.minD, lo, hi);
-                mask_labels<T>(cc, lo, hi, k);
+                for (int i = 0; i < 8; ++i) part[i] = gcombine<PYR>(s.L[i], vin[i]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) part[i] = s.L[i];
             }
-            gstep<T, PYR>(s, cc, cur.base, p2, p12, bufs + (t & 1) * G::BUFW, k);
-            const int ro = role(t, x);
-            uint32_t vin[4], tot[4] = {kMax2, kMax2, kMax2, kMax2};
-            to4(cur.v, vin);
-            uint4* slot = reinterpret_cast<uint4*>(band + (x - band_lo) * DW) + k;
-            uint4* vout = reinterpret_cast<uint4*>(J.V + ((size_t)yy * W + x) * D + 8 * k);
-            if (ro == 1) {
-                uint32_t part[4];
+            if (row_ok) st8(vp, part);
+        } else if (ro == 4) {
+            st8(mid + 8 * k, s.L);
+            defer = true;
+            xm = x;
+        } else if (ro == 2) {
+            uint32_t part[8], tot[8];
+            if (late(x)) ld8(vp, part);
+            else ld8(d + 8, part);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) part[i] = has_tb ? gcombine<PYR>(s.L[i], vin[i]) : s.L[i];
-                if (in_band(x)) *slot = from4(part);
-                else if (row_ok) *vout = from4(part);
-            } else if (ro == 4) {
-                reinterpret_cast<uint4*>(mid)[k] = from4(s.L);
-                defer = true;
-                xm = x;
-                base_m = cur.base;
-            } else if (ro == 2) {
-                uint32_t part[4];
-                if (in_band(x)) to4(*slot, part);
-                else to4(cur.v, part);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) tot[i] = gcombine<PYR>(part[i], s.L[i]);
-                if (J.debug_acc && row_ok) *vout = from4(tot);
-            } else if (ro == 3) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i) tot[i] = s.L[i];
-                if (J.debug_acc && row_ok) *vout = from4(tot);
-            }
-            const bool wta = (ro == 2 || ro == 3) && wta_px(x);
-            if (__any_sync(0xffffffffu, wta)) gwta<T, PYR>(J, wta && row_ok, yy, x, tot, cur.base, scr, lane, k);
+            for (int i = 0; i < 8; ++i) tot[i] = gcombine<PYR>(part[i], s.L[i]);
+            if (row_ok) st8(vp, tot);
+        } else if (ro == 3) {
+            if (row_ok) st8(vp, s.L);
         }
     }
+    cp_wait<0>();
     __syncwarp();
-    {
+    if (defer && row_ok) {
         // the pixel both paths reach at the same step: R->L finishes it
-        uint32_t tot[4] = {kMax2, kMax2, kMax2, kMax2};
-        bool wta = false;
-        if (defer) {
-            uint32_t part[4], lm[4];
-            to4(reinterpret_cast<const uint4*>(band + (xm - band_lo) * DW)[k], part);
-            to4(reinterpret_cast<const uint4*>(mid)[k], lm);
+        uint32_t part[8], lm[8], tot[8];
+        uint32_t* vp = reinterpret_cast<uint32_t*>(J.V + (prow + xm) * D + 16 * k);
+        ld8(vp, part);
+        ld8(mid + 8 * k, lm);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) tot[i] = gcombine<PYR>(part[i], lm[i]);
-            if (J.debug_acc && row_ok)
-                *reinterpret_cast<uint4*>(J.V + ((size_t)yy * W + xm) * D + 8 * k) = from4(tot);
-            wta = wta_px(xm);
-        }
-        if (__any_sync(0xffffffffu, wta)) gwta<T, PYR>(J, wta && row_ok, yy, xm, tot, base_m, scr, lane, k);
+        for (int i = 0; i < 8; ++i) tot[i] = gcombine<PYR>(part[i], lm[i]);
+        st8(vp, tot);
     }
-    // single-scale: pixels no path finishes stay invalid
-    if (!PYR && row_ok) {
-        const int16_t inv = (int16_t)((J.minD - 1) * 16);
-        for (int x = dir * T + k; x < W; x += 2 * T) {
-            if (wta_px(x)) continue;
-            J.disp_raw[(size_t)y * W + x] = inv;
-            J.conf_raw[(size_t)y * W + x] = 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// Winner-take-all of the packed levels, one thread per pixel, from the
+// totals of the three paths in V (kernel_WTA_Subpixel,
+// src/sgm_kernels.cu:573-640; pyramid kernel_PyramidWTA,
+// src/sgm_kernels.cu:1290-1370).  Keys (cost << 7 | label) order by cost,
+// then label, so one min tree gives the minimum and its first label.
+// Single-scale pixels outside [minD + D, w + min(minD, 0)) and the last
+// column are written invalid (no path finishes them in the reference).
+// ---------------------------------------------------------------------------
+template <int D, bool PYR, int NJ>
+__global__ void __launch_bounds__(256) k_wta(const __grid_constant__ Jobs<NJ> jobs)
+{
+    using namespace pk;
+    constexpr int DW = D / 2;
+    const LevelDesc& J = jobs.d[blockIdx.z];
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= J.w || y >= J.h) return;
+    const int W = J.w;
+    const size_t p = (size_t)y * W + x;
+    if (!PYR) {
+        const int minX1 = imax(J.minD + D, 0), maxX1 = W + imin(J.minD, 0);
+        if (!(x >= minX1 && x < maxX1 && x != W - 1)) {
+            J.disp_raw[p] = (int16_t)((J.minD - 1) * 16);
+            J.conf_raw[p] = 0.0f;
+            return;
         }
     }
+    const int16_t* tv = J.V + p * D;
+    uint32_t t[DW];
+#pragma unroll
+    for (int i = 0; i < DW / 4; ++i) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(tv) + i);
+        t[4 * i] = q.x; t[4 * i + 1] = q.y; t[4 * i + 2] = q.z; t[4 * i + 3] = q.w;
+    }
+    auto key = [&](int d) -> unsigned {
+        const uint32_t w = t[d >> 1];
+        return (((d & 1) ? (w >> 16) : (w & 0xffffu)) << 7) | (unsigned)d;
+    };
+    unsigned best = 0xffffffffu;
+#pragma unroll
+    for (int d = 0; d < D; d += 2) best = umin(best, umin(key(d), key(d + 1)));
+    const int minCost = (int)(best >> 7), bestD = (int)(best & 127u);
+    unsigned a = 0xffffffffu;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const bool near = (unsigned)(d - bestD + 1) <= 2u;
+        a = umin(a, near ? 0xffffffffu : key(d));
+    }
+    const int alt = (int)(a >> 7);
+    const int c0 = bestD > 0 ? (int)__ldg(tv + bestD - 1) : 0;
+    const int c2 = bestD + 1 < D ? (int)__ldg(tv + bestD + 1) : 0;
+    const int base = (PYR && J.refine) ? (int)J.base[p] : J.minD;
+    wta_out<D, PYR>(J, y, x, base, minCost, bestD, alt, c0, minCost, c2);
 }
 
 template <int T, bool PYR, int NJ>
@@ -513,18 +575,26 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         for (int i = 0; i < jobs.n; ++i)
             if (jobs.d[i].paths >= 3) tbj.d[n++] = jobs.d[i];
         tbj.n = n;
+        constexpr size_t smem = pk::tb_smem<T>();
+        if ((err = cudaFuncSetAttribute(k_gtb<T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+            cudaSuccess)
+            return err;
         const int cols = pk::kWarps * G::CPW;
         dim3 g((e.max_w + cols - 1) / cols, n);
         prof_begin(st);
-        k_gtb<T, PYR, NJ><<<g, pk::kWarps * 32, 0, st>>>(tbj);
+        k_gtb<T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(tbj);
         count_launch();
         prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * (tbj.d[0].refine ? 2 : 0), st);
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
     }
+    constexpr size_t smem = pk::row_smem<T>();
+    if ((err = cudaFuncSetAttribute(k_grow<T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return err;
     const int rows = pk::kWarps * G::CPW / 2;
     dim3 g((e.max_h + rows - 1) / rows, jobs.n);
     prof_begin(st);
-    k_grow<T, PYR, NJ><<<g, pk::kWarps * 32, 0, st>>>(jobs);
+    k_grow<T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(jobs);
     count_launch();
     if (prof_enabled()) {
         double by = 0;
@@ -535,6 +605,12 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         }
         prof_end(PK_PATH_ROW, by, st);
     }
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    dim3 gw((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
+    prof_begin(st);
+    k_wta<G::D, PYR, NJ><<<gw, 256, 0, st>>>(jobs);
+    count_launch();
+    prof_end(PK_WTA, jobs_vox(jobs) * 2 + jobs_px(jobs) * (6 + 4), st);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@ enum ProfKind {
     PK_PATH_ROW = 5,
     PK_POST = 6,
     PK_P2TABLE = 7,
+    PK_WTA = 8,
     PK_COUNT
 };
 
