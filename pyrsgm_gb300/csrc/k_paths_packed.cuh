@@ -393,78 +393,91 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     const bool has_lr = lr_n > 0, has_tb = J.paths >= 3;
     const int n_mine = dir == 0 ? lr_n : rl_n;
     const int Tn = imax(lr_n, rl_n);
-    const int C2 = W - 1 + lr_x0;   // 2x at the meeting point
-    // the first path left its partial less than S + 2 steps before: read it after the step's __syncwarp
-    auto late = [&](int x) { return abs(2 * x - C2) <= S + 1; };
-    auto lr_covers = [&](int x) { return has_lr && x >= lr_x0 && x < lr_x0 + lr_n; };
-    auto rl_covers = [&](int x) { return x >= W - rl_n; };
-    auto xpos = [&](int t) {
-        return dir == 0 ? lr_x0 + imin(t, imax(lr_n - 1, 0)) : W - 1 - imin(t, imax(rl_n - 1, 0));
-    };
-    // 0 nothing, 1 first at x, 2 second at x, 3 R->L alone, 4 R->L meets L->R at the same step
-    auto role = [&](int t, int x) -> int {
-        if (t >= n_mine) return 0;
-        if (dir == 0) return rl_covers(x) ? ((W - 1 - x) < t ? 2 : 1) : 0;
+    // Step t of this chain is at x = xs + dx * t.  With M = w - 1 - lr_x0 the
+    // L->R chain reaches x at step x - lr_x0 and the R->L chain at step
+    // w - 1 - x, so both are first for 2t < M and second for 2t > M; at
+    // 2t == M both reach the same pixel (L->R leaves its sum, R->L finishes
+    // after the walk).  R->L steps before t0 are outside the L->R range.
+    const int dx = dir == 0 ? 1 : -1;
+    const int xs = dir == 0 ? lr_x0 : W - 1;
+    const int M = W - 1 - lr_x0;
+    const int t0 = (dir == 1 && has_lr) ? W - lr_x0 - lr_n : 0;
+    // 0 nothing, 1 first, 2 second, 3 R->L alone, 4 R->L meets L->R at the same step
+    auto role = [&](int t) -> int {
+        if (t >= n_mine || t < t0) return 0;
         if (!has_lr) return 3;
-        if (!lr_covers(x)) return 0;
-        const int tl = x - lr_x0;
-        return tl < t ? 2 : (tl == t ? 4 : 1);
+        const int tt = 2 * t;
+        return tt < M ? 1 : (tt == M ? (dir ? 4 : 1) : 2);
     };
+    // the first chain left its partial less than S + 2 steps before: read it after the step's __syncwarp
+    auto late = [&](int t) { return abs(2 * t - M) <= S + 1; };
+    const int16_t* const Cg = J.C;
+    int16_t* const Vg = J.V;
+    const int16_t* const Bg = J.base;
+    const uint8_t* const Lg = J.left;
     const bool use_base = PYR && J.refine, adaptive = J.adaptive != 0;
+    const int P2c = J.P2, minD = J.minD;
     const size_t prow = (size_t)yy * W;
-    auto issue = [&](int t, int slot) {
-        const int x = xpos(t);
-        const int ro = role(t, x);
-        uint32_t* d = ring + slot * 32 * kRowRsw;
-        const size_t o = (prow + x) * D + 16 * k;
-        cp16(d, J.C + o);
-        cp16(d + 4, J.C + o + 8);
-        if ((ro == 1 && has_tb) || (ro == 2 && !late(x))) {
-            cp16(d + 8, J.V + o);
-            cp16(d + 12, J.V + o + 8);
+    const size_t lrow = (size_t)yy * J.lstep;
+    const long long dxD = (long long)dx * D;
+    // issue cursor (step ti) and consume cursor (step t): voxel offset, pixel index, image index
+    size_t oi = (prow + xs) * D + 16 * k, pi = prow + xs, li = lrow + xs;
+    size_t oc = oi, pc = pi, lc = li;
+    int ti = 0;
+    auto issue_next = [&](int slot) {
+        if (ti < n_mine) {
+            const int ro = role(ti);
+            uint32_t* d = ring + slot * 32 * kRowRsw;
+            cp16(d, Cg + oi);
+            cp16(d + 4, Cg + oi + 8);
+            if ((ro == 1 && has_tb) || (ro == 2 && !late(ti))) {
+                cp16(d + 8, Vg + oi);
+                cp16(d + 12, Vg + oi + 8);
+            }
+            if (use_base) cp4(d + 16, word_of(Bg + pi));
+            if (adaptive) cp4(d + 17, word_of(Lg + li));
         }
-        if (use_base) cp4(d + 16, word_of(J.base + prow + x));
-        if (adaptive) cp4(d + 17, word_of(J.left + (size_t)yy * J.lstep + x));
+        cp_commit();
+        ++ti;
+        oi += dxD;
+        pi += dx;
+        li += dx;
     };
 
     const uint32_t p12 = dup(imin(J.P1, 0x8000));
     GChain s;
-    gchain_init(s, J.minD);
+    gchain_init(s, minD);
 #pragma unroll
-    for (int j = 0; j < S - 1; ++j) {
-        if (j < n_mine) issue(j, j);
-        cp_commit();
-    }
+    for (int j = 0; j < S - 1; ++j) issue_next(j);
     int img_prev = 0, slot = 0, islot = S - 1;
     bool defer = false;
     int xm = 0;
     for (int t = 0; t < Tn; ++t) {
-        if (t + S - 1 < n_mine) issue(t + S - 1, islot);
-        cp_commit();
+        issue_next(islot);
         islot = islot + 1 == S ? 0 : islot + 1;
         cp_wait<S - 1>();
-        if (T == 1) __syncwarp();   // orders the other path's partial sums before the late reads below
+        if (T == 1) __syncwarp();   // orders the other chain's partial sums before the late reads below
         const uint32_t* d = ring + slot * 32 * kRowRsw;
         slot = slot + 1 == S ? 0 : slot + 1;
-        const int x = xpos(t);
+        const int x = xs + dx * t;
         uint32_t cc[8];
         ld8(d, cc);
-        const int base = use_base ? (int)(int16_t)(d[16] >> (((prow + x) & 1) * 16)) : J.minD;
-        int p2 = J.P2;
+        const int base = use_base ? (int)(int16_t)(d[16] >> ((pc & 1) * 16)) : minD;
+        int p2 = P2c;
         if (adaptive) {
-            const int img = (int)((d[17] >> byte_shift(J.left + (size_t)yy * J.lstep + x)) & 255u);
+            const int img = (int)((d[17] >> byte_shift(Lg + lc)) & 255u);
             p2 = lut[abs(img - img_prev) & 255];
             img_prev = img;
         }
         if (PYR && !J.refine) {
             int lo, hi;
-            label_range(J, x, J.minD, lo, hi);
+            label_range(J, x, minD, lo, hi);
             mask_labels(cc, lo, hi, k);
         }
         uint32_t* cw = chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0);
         gstep<T, PYR>(s, cc, base, p2, p12, cw, k);
-        const int ro = role(t, x);
-        uint32_t* vp = reinterpret_cast<uint32_t*>(J.V + (prow + x) * D + 16 * k);
+        const int ro = role(t);
+        uint32_t* vp = reinterpret_cast<uint32_t*>(Vg + oc);
         if (ro == 1) {
             uint32_t part[8];
             if (has_tb) {
@@ -483,7 +496,7 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
             xm = x;
         } else if (ro == 2) {
             uint32_t part[8], tot[8];
-            if (late(x)) ld8(vp, part);
+            if (late(t)) ld8(vp, part);
             else ld8(d + 8, part);
 #pragma unroll
             for (int i = 0; i < 8; ++i) tot[i] = gcombine<PYR>(part[i], s.L[i]);
@@ -491,13 +504,16 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
         } else if (ro == 3) {
             if (row_ok) st8(vp, s.L);
         }
+        oc += dxD;
+        pc += dx;
+        lc += dx;
     }
     cp_wait<0>();
     __syncwarp();
     if (defer && row_ok) {
         // the pixel both paths reach at the same step: R->L finishes it
         uint32_t part[8], lm[8], tot[8];
-        uint32_t* vp = reinterpret_cast<uint32_t*>(J.V + (prow + xm) * D + 16 * k);
+        uint32_t* vp = reinterpret_cast<uint32_t*>(Vg + (prow + xm) * D + 16 * k);
         ld8(vp, part);
         ld8(mid + 8 * k, lm);
 #pragma unroll
