@@ -9,12 +9,15 @@ reference's headline metric is quoted on).
 
   value   pairs/s with the inputs resident in device memory (CUDA events on
           the compute stream, L2 flushed between steps outside the events)
-  e2e     the same through the public API with pinned host buffers: per step
-          the host->device copy of every pair's images, compute(), and the
-          device->host copy of its three outputs, all inside the events
-  roofline  the dominant kernel (the row pass: L->R + R->L + WTA + LR check)
-          timed with CUDA events on its own stream via the library profiler,
-          its algorithmic bytes / duration against the measured HBM peak
+  e2e     the same through the public API with pinned host buffers: every
+          step copies its pairs' images host->device, runs the engine and
+          copies the three outputs device->host; two slots let one step's
+          copies overlap its neighbours' compute, and the events span all
+          steps, copies included
+  roofline  the dominant kernel (the row pass: L->R + R->L sums of the 16/32
+          label levels) timed with CUDA events on its stream via the library
+          profiler, its algorithmic bytes / duration against the measured
+          HBM peak
 
 --impl reference runs the reference's own CUDA kernels (compiled from its
 sources into oracle/_ref/ and launched by oracle/_build/libref_harness.so)
@@ -186,15 +189,70 @@ class BatchRunner(MineRunner):
     def step_direct(self, stream):
         self.engine.run_pairs(self.arr, False, stream)
 
-    def step_e2e(self, stream):
-        for i in range(len(self.costs)):
-            self.L[i].copy_(self.hL[i], non_blocking=True)
-            self.R[i].copy_(self.hR[i], non_blocking=True)
-        self.engine.run_pairs(self.arr, True, stream)
-        for i in range(len(self.costs)):
-            self.h16[i].copy_(self.d16[i], non_blocking=True)
-            self.h32[i].copy_(self.d32[i], non_blocking=True)
-            self.hcf[i].copy_(self.cf[i], non_blocking=True)
+    def e2e_begin(self, stream):
+        """Two slots of device inputs/outputs so that one step's copies overlap
+        the other's compute: H2D on one stream, the engine on the compute
+        stream, D2H on a third, ordered per slot by events."""
+        torch, pg = self.torch, self.pg
+        if getattr(self, "slots", None) is None:
+            self.slots = []
+            for k in range(2):
+                if k == 0:
+                    sl = dict(L=self.L, R=self.R, d16=self.d16, d32=self.d32, cf=self.cf, arr=self.arr)
+                else:
+                    sl = dict(L=[t.clone() for t in self.L], R=[t.clone() for t in self.R],
+                              d16=[torch.empty_like(t) for t in self.d16], d32=[torch.empty_like(t) for t in self.d32],
+                              cf=[torch.empty_like(t) for t in self.cf])
+                    items = [dict(left=sl["L"][i], right=sl["R"][i], params=pg.Params(**params_for(c)),
+                                  disp16=sl["d16"][i], disp32=sl["d32"][i], conf=sl["cf"][i])
+                             for i, c in enumerate(self.costs)]
+                    sl["arr"] = pg.BatchEngine.make_pairs(items)
+                    sl["hL"] = [torch.empty_like(t).pin_memory() for t in self.hL]
+                    sl["hR"] = [torch.empty_like(t).pin_memory() for t in self.hR]
+                    for a, b in zip(sl["hL"] + sl["hR"], self.hL + self.hR):
+                        a.copy_(b)
+                    sl["h16"] = [torch.empty_like(t).pin_memory() for t in self.h16]
+                    sl["h32"] = [torch.empty_like(t).pin_memory() for t in self.h32]
+                    sl["hcf"] = [torch.empty_like(t).pin_memory() for t in self.hcf]
+                if k == 0:
+                    sl.update(hL=self.hL, hR=self.hR, h16=self.h16, h32=self.h32, hcf=self.hcf)
+                sl["free"] = torch.cuda.Event()
+                sl["inp"] = torch.cuda.Event()
+                sl["done"] = torch.cuda.Event()
+                self.slots.append(sl)
+            self.s_h2d = torch.cuda.Stream()
+            self.s_d2h = torch.cuda.Stream()
+            self.engine.run_pairs(self.slots[1]["arr"], True, stream)   # graph for the second slot
+        start = torch.cuda.Event()
+        start.record(stream)
+        self.s_h2d.wait_event(start)
+        self.s_d2h.wait_event(start)
+        for sl in self.slots:
+            sl["free"].record(self.s_d2h)
+
+    def step_e2e(self, stream, k: int = 0):
+        torch = self.torch
+        sl = self.slots[k % 2]
+        with torch.cuda.stream(self.s_h2d):
+            self.s_h2d.wait_event(sl["free"])
+            for i in range(len(self.costs)):
+                sl["L"][i].copy_(sl["hL"][i], non_blocking=True)
+                sl["R"][i].copy_(sl["hR"][i], non_blocking=True)
+            sl["inp"].record(self.s_h2d)
+        stream.wait_event(sl["inp"])
+        self.engine.run_pairs(sl["arr"], True, stream)
+        sl["done"].record(stream)
+        with torch.cuda.stream(self.s_d2h):
+            self.s_d2h.wait_event(sl["done"])
+            for i in range(len(self.costs)):
+                sl["h16"][i].copy_(sl["d16"][i], non_blocking=True)
+                sl["h32"][i].copy_(sl["d32"][i], non_blocking=True)
+                sl["hcf"][i].copy_(sl["cf"][i], non_blocking=True)
+            sl["free"].record(self.s_d2h)
+
+    def e2e_end(self, stream):
+        stream.wait_stream(self.s_h2d)
+        stream.wait_stream(self.s_d2h)
 
 
 # ---------------------------------------------------------------------------
@@ -369,15 +427,36 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
         lib.pyrsgm_gb300_profile(0)
     total_ms = sum(step_ms)
     e2e_ms = []
-    for _ in range(max(1, args.steps // 2)):
+    if hasattr(runner, "e2e_begin"):
+        # pipelined: step k's H2D and D2H overlap the compute of its neighbours;
+        # the timed region spans all steps, copies included
+        n_e2e = max(2, args.steps)
         with torch.cuda.stream(stream):
             flush.fill_(2)
+            runner.e2e_begin(stream)
+            runner.step_e2e(stream, 0)   # untimed: settles both slots' graphs and pinned pages
+            runner.e2e_end(stream)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            runner.step_e2e(stream)
+            runner.e2e_begin(stream)
+            for k in range(n_e2e):
+                runner.step_e2e(stream, k)
+            runner.e2e_end(stream)
             b.record(stream)
         torch.cuda.synchronize()
-        e2e_ms.append(a.elapsed_time(b))
+        e2e_ms = [a.elapsed_time(b) / n_e2e] * n_e2e
+    else:
+        for _ in range(max(1, args.steps // 2)):
+            with torch.cuda.stream(stream):
+                flush.fill_(2)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                runner.step_e2e(stream)
+                b.record(stream)
+            torch.cuda.synchronize()
+            e2e_ms.append(a.elapsed_time(b))
     e2e_total = sum(e2e_ms)
     if world > 1:
         t = torch.tensor([total_ms, e2e_total], device=dev)
@@ -553,7 +632,7 @@ def run(args) -> dict | None:
         prof = headline["prof"]
         row = prof.get("path_row", {})
         achieved = (row["bytes"] / (row["ms"] / 1e3) / 1e9) if row.get("ms") else None
-        out["roofline"] = {"kernel": "k_path_row (L->R + R->L + WTA + disp2 + LR check)", "bound": "hbm",
+        out["roofline"] = {"kernel": "k_grow (L->R + R->L path sums, three-path totals)", "bound": "hbm",
                            "achieved": round(achieved, 2) if achieved else None, "peak": pk["hbm_gbs"],
                            "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4) if achieved else None,
                            "peak_source": pk["source"], "traffic": None,
@@ -604,7 +683,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=8, help="pairs per step")
+    ap.add_argument("--batch", type=int, default=16, help="pairs per step")
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--mode", choices=["batched", "plain", "serve"], default="batched",
                     help="headline execution: one batched run per step, or per-pair compute(); "

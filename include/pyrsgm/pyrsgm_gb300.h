@@ -176,6 +176,14 @@ const char* pyrsgm_gb300_version(void);
 /* Kernel launches issued by this library since the process started. */
 unsigned long long pyrsgm_gb300_launch_count(void);
 
+/* Shape of the 16/32/64-label aggregation kernels: 0 chooses per launch
+ * (one thread per 16 labels when the launch has rows enough to fill the
+ * GPU, else a chain spread over more threads), 8 forces the former, 2 or 4
+ * the latter.  Results are identical either way.  Returns the previous
+ * setting, or -1 for another value.  The environment variable
+ * PYRSGM_GB300_PACKED_NW gives the initial setting. */
+int pyrsgm_gb300_set_packed_words(int words);
+
 /* Per-kernel profiling with CUDA events recorded on each launch's stream.
  * pyrsgm_gb300_profile(1) clears the records and starts recording,
  * pyrsgm_gb300_profile(0) stops.  _read() waits for the recorded events of

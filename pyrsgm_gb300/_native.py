@@ -90,6 +90,7 @@ _SIGS = {
     "pyrsgm_gb300_server_inject_failure": (_i, [_vp, _i]),
     "pyrsgm_gb300_version": (C.c_char_p, []),
     "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
+    "pyrsgm_gb300_set_packed_words": (_i, [_i]),
     "pyrsgm_gb300_profile": (_i, [_i]),
     "pyrsgm_gb300_profile_read": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
 }

@@ -190,6 +190,15 @@ class StereoMatcher:
         return out
 
 
+def set_packed_words(words: int) -> int:
+    """Shape of the 16/32/64-label aggregation kernels (0 per launch, 8, or 2/4);
+    returns the previous setting.  Results do not depend on it."""
+    r = lib().pyrsgm_gb300_set_packed_words(int(words))
+    if r < 0:
+        raise ValueError("pyrsgm: packed words must be 0, 2, 4 or 8")
+    return r
+
+
 def pair_bytes(width: int, height: int, params: Params) -> int:
     """Device bytes one pair of this shape occupies (StereoMatcher or batch slot)."""
     return lib().pyrsgm_gb300_pair_bytes(width, height, C.byref(params.to_c()))

@@ -11,6 +11,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -25,6 +26,26 @@ static std::atomic<unsigned long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+static std::atomic<int> g_packed_words{[] {
+    const char* e = std::getenv("PYRSGM_GB300_PACKED_NW");
+    return e ? std::atoi(e) : 0;
+}()};
+int packed_words_override() { return g_packed_words.load(std::memory_order_relaxed); }
+
+int sm_count()
+{
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+    std::atomic<int>& slot = cache[dev & 63];
+    int n = slot.load(std::memory_order_relaxed);
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+        slot.store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
@@ -332,5 +353,11 @@ int pyrsgm_gb300_p2_table(int* d_table, int P2, float p2Alpha, float p2Beta, flo
 const char* pyrsgm_gb300_version(void) { return "0.1.0-gb300"; }
 
 unsigned long long pyrsgm_gb300_launch_count(void) { return pg::g_launches.load(std::memory_order_relaxed); }
+
+int pyrsgm_gb300_set_packed_words(int words)
+{
+    if (words != 0 && words != 2 && words != 4 && words != 8) return -1;
+    return pg::g_packed_words.exchange(words, std::memory_order_relaxed);
+}
 
 }  // extern "C"

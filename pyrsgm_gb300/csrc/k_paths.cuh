@@ -755,13 +755,37 @@ cudaError_t launch_paths_shape(const Jobs<NJ>& jobs, const LevelExtent& e, cudaS
     return cudaGetLastError();
 }
 
+// Words per thread of the packed kernels for a launch: 8 (one thread per
+// 16-label chain, the fewest instructions per pixel) when the launch has
+// rows enough for one such warp per SM, else the shorter-step shape
+// (2 words, or 4 for 64 labels).  packed_words_override() (set through
+// pyrsgm_gb300_set_packed_words) forces one of them.
+inline int packed_nw(int D, long long rows)
+{
+    const int force = packed_words_override();
+    const int small = D == 64 ? 4 : 2;
+    if (force == 8) return 8;
+    if (force == 2 || force == 4) return small;
+    const long long warps8 = rows * 2 * (D / 16) / 32;
+    return warps8 >= sm_count() ? 8 : small;
+}
+
 template <bool PYR, int NJ>
 cudaError_t launch_paths_mode(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
-    switch (path_variant(jobs.d[0].D)) {
-    case 10016: return launch_paths_packed<1, PYR, NJ>(jobs, e, st);
-    case 10032: return launch_paths_packed<2, PYR, NJ>(jobs, e, st);
-    case 10064: return launch_paths_packed<4, PYR, NJ>(jobs, e, st);
+    long long rows = 0;
+    for (int i = 0; i < jobs.n; ++i) rows += jobs.d[i].h;
+    const int D = jobs.d[0].D;
+    switch (path_variant(D)) {
+    case 10016:
+        return packed_nw(D, rows) == 8 ? launch_paths_packed<8, 1, PYR, NJ>(jobs, e, st)
+                                       : launch_paths_packed<2, 4, PYR, NJ>(jobs, e, st);
+    case 10032:
+        return packed_nw(D, rows) == 8 ? launch_paths_packed<8, 2, PYR, NJ>(jobs, e, st)
+                                       : launch_paths_packed<2, 8, PYR, NJ>(jobs, e, st);
+    case 10064:
+        return packed_nw(D, rows) == 8 ? launch_paths_packed<8, 4, PYR, NJ>(jobs, e, st)
+                                       : launch_paths_packed<4, 8, PYR, NJ>(jobs, e, st);
     case 1601: return launch_paths_shape<16, 1, PYR, NJ>(jobs, e, st);
     case 3201: return launch_paths_shape<32, 1, PYR, NJ>(jobs, e, st);
     case 3202: return launch_paths_shape<32, 2, PYR, NJ>(jobs, e, st);

@@ -1,7 +1,9 @@
-// k_paths_packed.cuh -- path aggregation for D = 16*T labels (16, 32, 64):
-// the labels of one path chain are packed two per 32-bit word and held by
-// T threads, eight words (sixteen labels) each; T = 1 for the 16-label
-// refine levels, so a chain is one thread.
+// k_paths_packed.cuh -- path aggregation for D = 2*NW*T labels (16, 32,
+// 64): the labels of one path chain are packed two per 32-bit word and held
+// by T threads, NW words each.  NW = 8 (a 16-label chain is one thread)
+// spends the fewest instructions per pixel and suits launches with many
+// rows; NW = 2 spreads a chain over more threads, shortening each step, for
+// launches with few rows (one pair, coarse levels).
 //
 // The recurrence of a step (reference: src/sgm_kernels.cu:560-565
 // single-scale, 1230-1252 pyramid) runs on 16-bit pairs with the DPX
@@ -23,9 +25,9 @@
 //   * an active chain whose best is SHRT_MAX gives SHRT_MAX (the sign of
 //     best + 1 per half, replicated by prmt).
 //
-// Shifted windows: each step a thread stores its eight words of the
+// Shifted windows: each step a thread stores its NW words of the
 // previous step into its chain's guard-padded shared buffer and reads back
-// the ten words of its shifted window (word w of chain c at w * CPW + c, so
+// the NW + 2 words of its shifted window (word w of chain c at w * CPW + c, so
 // a one-thread chain touches only its own bank).  Chains of T > 1 threads
 // double-buffer the window and exchange it with one __syncwarp per step;
 // their minima and argmins reduce by __shfl_xor_sync.
@@ -60,8 +62,6 @@ constexpr uint32_t kOne2 = 0x00010001u;
 constexpr int kWarps = 4;        // warps per block
 constexpr int kStages = 6;       // look-ahead of the horizontal pass (steps)
 constexpr int kStagesTb = 8;     // look-ahead of the top->bottom pass
-constexpr int kRowRsw = 20;      // ring words per thread and stage: c[8] v[8] base img (+2: conflict-free 16-B lanes)
-constexpr int kTbRsw = 12;       // c[8] base img (+2)
 
 __device__ __forceinline__ uint32_t dup(int v) { return ((uint32_t)v & 0xffffu) * 0x10001u; }
 
@@ -77,6 +77,10 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)
 __device__ __forceinline__ void cp16(void* dst, const void* src)
 {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp8(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp4(void* dst, const void* src)
 {
@@ -96,57 +100,120 @@ __device__ __forceinline__ const void* word_of(const void* p)
 }
 __device__ __forceinline__ int byte_shift(const void* p) { return (int)(reinterpret_cast<uintptr_t>(p) & 3) * 8; }
 
-template <int T>
+template <int NW, int T>
 struct Grp {
-    static constexpr int D = 16 * T;            // labels per chain
+    static constexpr int D = 2 * NW * T;        // labels per chain
     static constexpr int CPW = 32 / T;          // chains per warp
     static constexpr int PADW = D / 2 + 1;      // guard words before label 0 (D + 2 halves)
     static constexpr int LENW = PADW + D + 2;   // words a shifted window can touch
     static constexpr int BUFW = LENW * CPW;     // one window buffer of a warp
     static constexpr int NBUF = T == 1 ? 1 : 2;
+    // Ring slot of a thread: costs [0, NW), partial sums [NW, 2NW), label
+    // base word, image word; strides chosen so that the 16- or 8-byte lane
+    // accesses of a warp hit distinct banks.
+    static constexpr int RSW = NW == 8 ? 20 : (NW == 4 ? 12 : 6);
+    static constexpr int RSW_TB = NW == 2 ? 6 : 12;   // costs, base, image
 };
 
+template <int NW>
 struct GChain {
-    uint32_t L[8];
+    uint32_t L[NW];
     int mp;        // minimum of the previous step over the chain's labels
     int prevBase;
 };
 
-__device__ __forceinline__ void gchain_init(GChain& s, int minD)
+template <int NW>
+__device__ __forceinline__ void gchain_init(GChain<NW>& s, int minD)
 {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) s.L[i] = kMax2;
+    for (int i = 0; i < NW; ++i) s.L[i] = kMax2;
     s.mp = 0x7fff;
     s.prevBase = minD;
 }
 
-// One step of the chain: c = this thread's sixteen costs of the pixel,
+// NW consecutive words (16-byte aligned for NW >= 4, 8-byte for NW == 2).
+template <int NW>
+__device__ __forceinline__ void ldw(const uint32_t* p, uint32_t (&v)[NW])
+{
+    if constexpr (NW == 2) {
+        const uint2 a = *reinterpret_cast<const uint2*>(p);
+        v[0] = a.x; v[1] = a.y;
+    } else {
+#pragma unroll
+        for (int i = 0; i < NW / 4; ++i) {
+            const uint4 a = reinterpret_cast<const uint4*>(p)[i];
+            v[4 * i] = a.x; v[4 * i + 1] = a.y; v[4 * i + 2] = a.z; v[4 * i + 3] = a.w;
+        }
+    }
+}
+template <int NW>
+__device__ __forceinline__ void stw(uint32_t* p, const uint32_t (&v)[NW])
+{
+    if constexpr (NW == 2) {
+        *reinterpret_cast<uint2*>(p) = make_uint2(v[0], v[1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < NW / 4; ++i)
+            reinterpret_cast<uint4*>(p)[i] = make_uint4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    }
+}
+// Asynchronous copy of NW words.
+template <int NW>
+__device__ __forceinline__ void cpw(uint32_t* dst, const int16_t* src)
+{
+    if constexpr (NW == 2) {
+        cp8(dst, src);
+    } else {
+#pragma unroll
+        for (int i = 0; i < NW / 4; ++i) cp16(dst + 4 * i, src + 8 * i);
+    }
+}
+
+// Minimum over the chain's words: a tree in the thread, then over the group.
+template <int NW, int T>
+__device__ __forceinline__ uint32_t chain_min2(const uint32_t (&L)[NW])
+{
+    uint32_t m2;
+    if constexpr (NW == 2) {
+        m2 = __vminu2(L[0], L[1]);
+    } else if constexpr (NW == 4) {
+        m2 = __vimin3_u16x2(L[0], L[1], __vminu2(L[2], L[3]));
+    } else {
+        m2 = __vminu2(__vimin3_u16x2(L[0], L[1], L[2]), __vimin3_u16x2(L[3], L[4], L[5]));
+        m2 = __vimin3_u16x2(m2, L[6], L[7]);
+    }
+#pragma unroll
+    for (int o = 1; o < T; o <<= 1) m2 = __vminu2(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    return m2;
+}
+
+// One step of the chain: c = this thread's 2*NW costs of the pixel,
 // buf = word 0 of the chain's window buffer (this step's parity).
-template <int T, bool PYR>
-__device__ __forceinline__ void gstep(GChain& s, const uint32_t (&c)[8], int base, int p2, uint32_t p12,
+template <int NW, int T, bool PYR>
+__device__ __forceinline__ void gstep(GChain<NW>& s, const uint32_t (&c)[NW], int base, int p2, uint32_t p12,
                                       uint32_t* buf, int k)
 {
-    using G = Grp<T>;
+    using G = Grp<NW, T>;
     constexpr int D = G::D, ST = G::CPW;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) buf[(G::PADW + 8 * k + i) * ST] = s.L[i];
+    for (int i = 0; i < NW; ++i) buf[(G::PADW + NW * k + i) * ST] = s.L[i];
     if (T > 1) __syncwarp();
     int delta = PYR ? base - s.prevBase : 0;
     delta = iclamp(delta, -(D + 1), D + 1);
-    const int i0 = 2 * G::PADW + delta - 1 + 16 * k;   // half index of label (16k - 1) after the shift
+    const int i0 = 2 * G::PADW + delta - 1 + 2 * NW * k;   // half index of label (2NW*k - 1) after the shift
     const uint32_t* wp = buf + (i0 >> 1) * ST;
     const uint32_t sh = (uint32_t)(i0 & 1) * 16;
-    uint32_t w0[10];
+    uint32_t w0[NW + 2];
 #pragma unroll
-    for (int j = 0; j < 10; ++j) w0[j] = wp[j * ST];
-    uint32_t w[9];
+    for (int j = 0; j < NW + 2; ++j) w0[j] = wp[j * ST];
+    uint32_t w[NW + 1];
 #pragma unroll
-    for (int j = 0; j < 9; ++j) w[j] = __funnelshift_r(w0[j], w0[j + 1], sh);
+    for (int j = 0; j < NW + 1; ++j) w[j] = __funnelshift_r(w0[j], w0[j + 1], sh);
     const int lj = imin(0x7fff, s.mp + p2);
     const uint32_t lj2 = dup(lj), mp2 = dup(s.mp);
     const uint32_t inc2 = (PYR && s.mp < 0x7fff) ? kOne2 : 0u;
 #pragma unroll
-    for (int m = 0; m < 8; ++m) {
+    for (int m = 0; m < NW; ++m) {
         const uint32_t n0 = __funnelshift_r(w[m], w[m + 1], 16);   // (L[s], L[s+1])
         const uint32_t t = __viaddmin_u16x2(w[m], p12, lj2);       // min(L[s-1] + P1, lj)
         const uint32_t best = __vimin3_u16x2(n0, t, w[m + 1] + p12);
@@ -154,22 +221,21 @@ __device__ __forceinline__ void gstep(GChain& s, const uint32_t (&c)[8], int bas
         if constexpr (PYR) v |= sign_mask2(best + inc2) & kMax2;
         s.L[m] = v;
     }
-    uint32_t m2 = __vminu2(__vimin3_u16x2(s.L[0], s.L[1], s.L[2]), __vimin3_u16x2(s.L[3], s.L[4], s.L[5]));
-    m2 = __vimin3_u16x2(m2, s.L[6], s.L[7]);
-#pragma unroll
-    for (int o = 1; o < T; o <<= 1) m2 = __vminu2(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    const uint32_t m2 = chain_min2<NW, T>(s.L);
     s.mp = imin((int)(m2 & 0xffffu), (int)(m2 >> 16));
     s.prevBase = base;
 }
 
 // Coarse pyramid levels: labels outside label_range take SHRT_MAX.
-__device__ __forceinline__ void mask_labels(uint32_t (&c)[8], int lo, int hi, int k)
+template <int NW>
+__device__ __forceinline__ void mask_labels(uint32_t (&c)[NW], int lo, int hi, int k)
 {
-    if (lo <= 16 * k && hi >= 16 * k + 15) return;
+    const int d0 = 2 * NW * k;
+    if (lo <= d0 && hi >= d0 + 2 * NW - 1) return;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const int d0 = 16 * k + 2 * i;
-        const bool ok0 = d0 >= lo && d0 <= hi, ok1 = d0 + 1 >= lo && d0 + 1 <= hi;
+    for (int i = 0; i < NW; ++i) {
+        const int d = d0 + 2 * i;
+        const bool ok0 = d >= lo && d <= hi, ok1 = d + 1 >= lo && d + 1 <= hi;
         c[i] |= (ok0 ? 0u : 0x7fffu) | (ok1 ? 0u : 0x7fff0000u);
     }
 }
@@ -185,17 +251,6 @@ __device__ __forceinline__ uint32_t gcombine(uint32_t a, uint32_t b)
     } else {
         return __viaddmin_u16x2(a, b, kMax2);
     }
-}
-
-__device__ __forceinline__ void ld8(const uint32_t* p, uint32_t (&v)[8])
-{
-    const uint4 a = reinterpret_cast<const uint4*>(p)[0], b = reinterpret_cast<const uint4*>(p)[1];
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-}
-__device__ __forceinline__ void st8(uint32_t* p, const uint32_t (&v)[8])
-{
-    reinterpret_cast<uint4*>(p)[0] = make_uint4(v[0], v[1], v[2], v[3]);
-    reinterpret_cast<uint4*>(p)[1] = make_uint4(v[4], v[5], v[6], v[7]);
 }
 
 // Outputs of a winner (kernel_WTA_Subpixel, src/sgm_kernels.cu:573-640;
@@ -258,17 +313,17 @@ __device__ __forceinline__ void wta_out(const LevelDesc& J, int y, int x, int ba
     J.conf_raw[p] = cout;
 }
 
-template <int T>
+template <int NW, int T>
 constexpr size_t row_smem()
 {
-    using G = Grp<T>;
-    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStages * 32 * kRowRsw + (G::CPW / 2) * (G::D / 2));
+    using G = Grp<NW, T>;
+    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStages * 32 * G::RSW + (G::CPW / 2) * (G::D / 2));
 }
-template <int T>
+template <int NW, int T>
 constexpr size_t tb_smem()
 {
-    using G = Grp<T>;
-    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStagesTb * 32 * kTbRsw);
+    using G = Grp<NW, T>;
+    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStagesTb * 32 * G::RSW_TB);
 }
 
 }  // namespace pk
@@ -276,12 +331,12 @@ constexpr size_t tb_smem()
 // ---------------------------------------------------------------------------
 // Top -> bottom: a warp holds 32/T adjacent columns, T threads each.
 // ---------------------------------------------------------------------------
-template <int T, bool PYR, int NJ>
+template <int NW, int T, bool PYR, int NJ>
 __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__ Jobs<NJ> jobs)
 {
     using namespace pk;
-    using G = Grp<T>;
-    constexpr int D = G::D, S = kStagesTb;
+    using G = Grp<NW, T>;
+    constexpr int D = G::D, S = kStagesTb, RS = G::RSW_TB;
     const LevelDesc& J = jobs.d[blockIdx.y];
     extern __shared__ __align__(16) uint32_t smem[];
     int* lut = reinterpret_cast<int*>(smem);
@@ -301,48 +356,59 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
     const bool col_ok = col < ncol;
     const int x = xlo + imin(col, ncol - 1), H = J.h, W = J.w;
     uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
-    uint32_t* ring = rbuf + (warp * S * 32 + lane) * kTbRsw;
+    uint32_t* ring = rbuf + (warp * S * 32 + lane) * RS;
     const uint32_t p12 = dup(imin(J.P1, 0x8000));
     int lo = 0, hi = D - 1;
     if (PYR && !J.refine) label_range(J, x, J.minD, lo, hi);
     const bool use_base = PYR && J.refine, adaptive = J.adaptive != 0;
-    const int16_t* cp = J.C + (size_t)x * D + 16 * k;
-    const size_t cstep = (size_t)W * D;
-    auto issue = [&](int y, int slot) {
-        uint32_t* d = ring + slot * 32 * kTbRsw;
-        const int16_t* src = cp + (size_t)y * cstep;
-        cp16(d, src);
-        cp16(d + 4, src + 8);
-        if (use_base) cp4(d + 8, word_of(J.base + (size_t)y * W + x));
-        if (adaptive) cp4(d + 9, word_of(J.left + (size_t)y * J.lstep + x));
+    const int16_t* const Cg = J.C;
+    int16_t* const Vg = J.V;
+    const int16_t* const Bg = J.base;
+    const uint8_t* const Lg = J.left;
+    const size_t vstep = (size_t)W * D, lstep = (size_t)J.lstep;
+    // issue cursor (row yi) and consume cursor (row y)
+    size_t oi = (size_t)x * D + 2 * NW * k, pi = x, li = x;
+    size_t oc = oi, pc = pi, lc = li;
+    int yi = 0;
+    auto issue_next = [&](int slot) {
+        if (yi < H) {
+            uint32_t* d = ring + slot * 32 * RS;
+            cpw<NW>(d, Cg + oi);
+            if (use_base) cp4(d + NW, word_of(Bg + pi));
+            if (adaptive) cp4(d + NW + 1, word_of(Lg + li));
+        }
+        cp_commit();
+        ++yi;
+        oi += vstep;
+        pi += W;
+        li += lstep;
     };
-    GChain s;
+    GChain<NW> s;
     gchain_init(s, J.minD);
 #pragma unroll
-    for (int j = 0; j < S - 1; ++j) {
-        if (j < H) issue(j, j);
-        cp_commit();
-    }
+    for (int j = 0; j < S - 1; ++j) issue_next(j);
     int img_prev = 0, slot = 0, islot = S - 1;
     for (int y = 0; y < H; ++y) {
-        if (y + S - 1 < H) issue(y + S - 1, islot);
-        cp_commit();
+        issue_next(islot);
         islot = islot + 1 == S ? 0 : islot + 1;
         cp_wait<S - 1>();
-        const uint32_t* d = ring + slot * 32 * kTbRsw;
+        const uint32_t* d = ring + slot * 32 * RS;
         slot = slot + 1 == S ? 0 : slot + 1;
-        uint32_t cc[8];
-        ld8(d, cc);
-        const int base = use_base ? (int)(int16_t)(d[8] >> ((((size_t)y * W + x) & 1) * 16)) : J.minD;
+        uint32_t cc[NW];
+        ldw<NW>(d, cc);
+        const int base = use_base ? (int)(int16_t)(d[NW] >> ((pc & 1) * 16)) : J.minD;
         int p2 = J.P2;
         if (adaptive) {
-            const int img = (int)((d[9] >> byte_shift(J.left + (size_t)y * J.lstep + x)) & 255u);
+            const int img = (int)((d[NW + 1] >> byte_shift(Lg + lc)) & 255u);
             p2 = lut[abs(img - img_prev) & 255];
             img_prev = img;
         }
-        if (PYR && !J.refine) mask_labels(cc, lo, hi, k);
-        gstep<T, PYR>(s, cc, base, p2, p12, chain + (G::NBUF == 2 ? (y & 1) * G::BUFW : 0), k);
-        if (col_ok) st8(reinterpret_cast<uint32_t*>(J.V + (size_t)y * cstep + (size_t)x * D + 16 * k), s.L);
+        if (PYR && !J.refine) mask_labels<NW>(cc, lo, hi, k);
+        gstep<NW, T, PYR>(s, cc, base, p2, p12, chain + (G::NBUF == 2 ? (y & 1) * G::BUFW : 0), k);
+        if (col_ok) stw<NW>(reinterpret_cast<uint32_t*>(Vg + oc), s.L);
+        oc += vstep;
+        pc += W;
+        lc += lstep;
     }
     cp_wait<0>();
 }
@@ -351,18 +417,18 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
 // Horizontal pass: a warp holds 16/T rows; per row an L->R group and an
 // R->L group of T threads.
 // ---------------------------------------------------------------------------
-template <int T, bool PYR, int NJ>
+template <int NW, int T, bool PYR, int NJ>
 __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant__ Jobs<NJ> jobs)
 {
     using namespace pk;
-    using G = Grp<T>;
-    constexpr int D = G::D, RPW = G::CPW / 2, S = kStages;
+    using G = Grp<NW, T>;
+    constexpr int D = G::D, RPW = G::CPW / 2, S = kStages, RS = G::RSW;
     const LevelDesc& J = jobs.d[blockIdx.y];
     extern __shared__ __align__(16) uint32_t smem[];
     int* lut = reinterpret_cast<int*>(smem);
     uint32_t* cbuf = smem + 256;
     uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
-    uint32_t* mbuf = rbuf + kWarps * S * 32 * kRowRsw;
+    uint32_t* mbuf = rbuf + kWarps * S * 32 * RS;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
     for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
     __syncthreads();
@@ -375,17 +441,16 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     const int yy = imin(y, J.h - 1);
     const int W = J.w;
     uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
-    uint32_t* ring = rbuf + (warp * S * 32 + lane) * kRowRsw;
+    uint32_t* ring = rbuf + (warp * S * 32 + lane) * RS;
     uint32_t* mid = mbuf + (warp * RPW + r) * (D / 2);
 
     // path extents (single-scale: kernel_AggregateLR/RL ranges)
-    int minX1 = 0, maxX1 = W, lr_x0 = 0, lr_n, rl_n;
+    int lr_x0 = 0, lr_n, rl_n;
     if (PYR) {
         lr_n = J.paths >= 2 ? W : 0;
         rl_n = W;
     } else {
-        minX1 = imax(J.minD + D, 0);
-        maxX1 = W + imin(J.minD, 0);
+        const int minX1 = imax(J.minD + D, 0), maxX1 = W + imin(J.minD, 0);
         lr_x0 = minX1;
         lr_n = J.paths >= 2 ? imax(0, maxX1 - minX1) : 0;
         rl_n = imax(0, W - minX1);
@@ -421,21 +486,17 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     const size_t lrow = (size_t)yy * J.lstep;
     const long long dxD = (long long)dx * D;
     // issue cursor (step ti) and consume cursor (step t): voxel offset, pixel index, image index
-    size_t oi = (prow + xs) * D + 16 * k, pi = prow + xs, li = lrow + xs;
+    size_t oi = (prow + xs) * D + 2 * NW * k, pi = prow + xs, li = lrow + xs;
     size_t oc = oi, pc = pi, lc = li;
     int ti = 0;
     auto issue_next = [&](int slot) {
         if (ti < n_mine) {
             const int ro = role(ti);
-            uint32_t* d = ring + slot * 32 * kRowRsw;
-            cp16(d, Cg + oi);
-            cp16(d + 4, Cg + oi + 8);
-            if ((ro == 1 && has_tb) || (ro == 2 && !late(ti))) {
-                cp16(d + 8, Vg + oi);
-                cp16(d + 12, Vg + oi + 8);
-            }
-            if (use_base) cp4(d + 16, word_of(Bg + pi));
-            if (adaptive) cp4(d + 17, word_of(Lg + li));
+            uint32_t* d = ring + slot * 32 * RS;
+            cpw<NW>(d, Cg + oi);
+            if ((ro == 1 && has_tb) || (ro == 2 && !late(ti))) cpw<NW>(d + NW, Vg + oi);
+            if (use_base) cp4(d + 2 * NW, word_of(Bg + pi));
+            if (adaptive) cp4(d + 2 * NW + 1, word_of(Lg + li));
         }
         cp_commit();
         ++ti;
@@ -445,7 +506,7 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     };
 
     const uint32_t p12 = dup(imin(J.P1, 0x8000));
-    GChain s;
+    GChain<NW> s;
     gchain_init(s, minD);
 #pragma unroll
     for (int j = 0; j < S - 1; ++j) issue_next(j);
@@ -457,52 +518,52 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
         islot = islot + 1 == S ? 0 : islot + 1;
         cp_wait<S - 1>();
         if (T == 1) __syncwarp();   // orders the other chain's partial sums before the late reads below
-        const uint32_t* d = ring + slot * 32 * kRowRsw;
+        const uint32_t* d = ring + slot * 32 * RS;
         slot = slot + 1 == S ? 0 : slot + 1;
         const int x = xs + dx * t;
-        uint32_t cc[8];
-        ld8(d, cc);
-        const int base = use_base ? (int)(int16_t)(d[16] >> ((pc & 1) * 16)) : minD;
+        uint32_t cc[NW];
+        ldw<NW>(d, cc);
+        const int base = use_base ? (int)(int16_t)(d[2 * NW] >> ((pc & 1) * 16)) : minD;
         int p2 = P2c;
         if (adaptive) {
-            const int img = (int)((d[17] >> byte_shift(Lg + lc)) & 255u);
+            const int img = (int)((d[2 * NW + 1] >> byte_shift(Lg + lc)) & 255u);
             p2 = lut[abs(img - img_prev) & 255];
             img_prev = img;
         }
         if (PYR && !J.refine) {
             int lo, hi;
             label_range(J, x, minD, lo, hi);
-            mask_labels(cc, lo, hi, k);
+            mask_labels<NW>(cc, lo, hi, k);
         }
         uint32_t* cw = chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0);
-        gstep<T, PYR>(s, cc, base, p2, p12, cw, k);
+        gstep<NW, T, PYR>(s, cc, base, p2, p12, cw, k);
         const int ro = role(t);
         uint32_t* vp = reinterpret_cast<uint32_t*>(Vg + oc);
         if (ro == 1) {
-            uint32_t part[8];
+            uint32_t part[NW];
             if (has_tb) {
-                uint32_t vin[8];
-                ld8(d + 8, vin);
+                uint32_t vin[NW];
+                ldw<NW>(d + NW, vin);
 #pragma unroll
-                for (int i = 0; i < 8; ++i) part[i] = gcombine<PYR>(s.L[i], vin[i]);
+                for (int i = 0; i < NW; ++i) part[i] = gcombine<PYR>(s.L[i], vin[i]);
             } else {
 #pragma unroll
-                for (int i = 0; i < 8; ++i) part[i] = s.L[i];
+                for (int i = 0; i < NW; ++i) part[i] = s.L[i];
             }
-            if (row_ok) st8(vp, part);
+            if (row_ok) stw<NW>(vp, part);
         } else if (ro == 4) {
-            st8(mid + 8 * k, s.L);
+            stw<NW>(mid + NW * k, s.L);
             defer = true;
             xm = x;
         } else if (ro == 2) {
-            uint32_t part[8], tot[8];
-            if (late(t)) ld8(vp, part);
-            else ld8(d + 8, part);
+            uint32_t part[NW], tot[NW];
+            if (late(t)) ldw<NW>(vp, part);
+            else ldw<NW>(d + NW, part);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) tot[i] = gcombine<PYR>(part[i], s.L[i]);
-            if (row_ok) st8(vp, tot);
+            for (int i = 0; i < NW; ++i) tot[i] = gcombine<PYR>(part[i], s.L[i]);
+            if (row_ok) stw<NW>(vp, tot);
         } else if (ro == 3) {
-            if (row_ok) st8(vp, s.L);
+            if (row_ok) stw<NW>(vp, s.L);
         }
         oc += dxD;
         pc += dx;
@@ -512,13 +573,13 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     __syncwarp();
     if (defer && row_ok) {
         // the pixel both paths reach at the same step: R->L finishes it
-        uint32_t part[8], lm[8], tot[8];
-        uint32_t* vp = reinterpret_cast<uint32_t*>(Vg + (prow + xm) * D + 16 * k);
-        ld8(vp, part);
-        ld8(mid + 8 * k, lm);
+        uint32_t part[NW], lm[NW], tot[NW];
+        uint32_t* vp = reinterpret_cast<uint32_t*>(Vg + (prow + xm) * D + 2 * NW * k);
+        ldw<NW>(vp, part);
+        ldw<NW>(mid + NW * k, lm);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) tot[i] = gcombine<PYR>(part[i], lm[i]);
-        st8(vp, tot);
+        for (int i = 0; i < NW; ++i) tot[i] = gcombine<PYR>(part[i], lm[i]);
+        stw<NW>(vp, tot);
     }
 }
 
@@ -578,10 +639,10 @@ __global__ void __launch_bounds__(256) k_wta(const __grid_constant__ Jobs<NJ> jo
     wta_out<D, PYR>(J, y, x, base, minCost, bestD, alt, c0, minCost, c2);
 }
 
-template <int T, bool PYR, int NJ>
+template <int NW, int T, bool PYR, int NJ>
 cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
-    using G = pk::Grp<T>;
+    using G = pk::Grp<NW, T>;
     cudaError_t err;
     bool any_tb = false;
     for (int i = 0; i < jobs.n; ++i) any_tb = any_tb || jobs.d[i].paths >= 3;
@@ -591,33 +652,36 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         for (int i = 0; i < jobs.n; ++i)
             if (jobs.d[i].paths >= 3) tbj.d[n++] = jobs.d[i];
         tbj.n = n;
-        constexpr size_t smem = pk::tb_smem<T>();
-        if ((err = cudaFuncSetAttribute(k_gtb<T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-            cudaSuccess)
+        constexpr size_t smem = pk::tb_smem<NW, T>();
+        if ((err = cudaFuncSetAttribute(k_gtb<NW, T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem)) != cudaSuccess)
             return err;
         const int cols = pk::kWarps * G::CPW;
         dim3 g((e.max_w + cols - 1) / cols, n);
         prof_begin(st);
-        k_gtb<T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(tbj);
+        k_gtb<NW, T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(tbj);
         count_launch();
-        prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * (tbj.d[0].refine ? 2 : 0), st);
+        prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * ((tbj.d[0].refine ? 2 : 0) + (tbj.d[0].adaptive ? 1 : 0)), st);
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
     }
-    constexpr size_t smem = pk::row_smem<T>();
-    if ((err = cudaFuncSetAttribute(k_grow<T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+    constexpr size_t smem = pk::row_smem<NW, T>();
+    if ((err = cudaFuncSetAttribute(k_grow<NW, T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
         cudaSuccess)
         return err;
     const int rows = pk::kWarps * G::CPW / 2;
     dim3 g((e.max_h + rows - 1) / rows, jobs.n);
     prof_begin(st);
-    k_grow<T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(jobs);
+    k_grow<NW, T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(jobs);
     count_launch();
     if (prof_enabled()) {
+        // algorithmic bytes: both horizontal paths read the cost volume, the
+        // top->bottom sums are read once and the totals written once (the
+        // partial sums of the meeting scheme are extra traffic, not counted)
         double by = 0;
         for (int i = 0; i < jobs.n; ++i) {
             const LevelDesc& d = jobs.d[i];
             const double px = (double)d.w * d.h;
-            by += px * d.D * (2 + (d.paths >= 3 ? 2 : 0)) + px * (6 + (d.refine ? 2 : 0));
+            by += px * d.D * 2 * (2 + (d.paths >= 3 ? 1 : 0) + 1) + px * 2 * ((d.refine ? 2 : 0) + (d.adaptive ? 1 : 0));
         }
         prof_end(PK_PATH_ROW, by, st);
     }
@@ -626,7 +690,7 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     prof_begin(st);
     k_wta<G::D, PYR, NJ><<<gw, 256, 0, st>>>(jobs);
     count_launch();
-    prof_end(PK_WTA, jobs_vox(jobs) * 2 + jobs_px(jobs) * (6 + 4), st);
+    prof_end(PK_WTA, jobs_vox(jobs) * 2 + jobs_px(jobs) * (2 + 6 + 4), st);
     return cudaGetLastError();
 }
 

@@ -84,6 +84,11 @@ inline int path_variant(int D)
     return s.G * 100 + s.K;
 }
 
+// Multiprocessor count of the current device (cached per device).
+int sm_count();
+// 0 (choose per launch), 8, or 2/4: the packed kernels' words per thread.
+int packed_words_override();
+
 // Count of kernel launches issued by this library (process-wide); a CUDA
 // graph replay counts the kernels it contains.
 void count_launch();

@@ -81,3 +81,25 @@ def test_p2_table_matches_libm_closely():
         dev = _runners.device_lut(case)
         host = _oracle.p2_table_libm(P2, *a)
         assert np.max(np.abs(dev.astype(np.int64) - host)) <= 1
+
+
+PACKED = [c for c in cases.SINGLE_SCALE + cases.LEVELS if c["D"] in (16, 32, 64)]
+
+
+@pytest.mark.parametrize("words", [8, 2])
+@pytest.mark.parametrize("case", PACKED, ids=[c["name"] for c in PACKED])
+def test_packed_shapes_match_reference(case, words):
+    """Both shapes of the 16/32/64-label kernels (one thread per 16 labels,
+    or a chain spread over several threads) give the reference's results."""
+    import pyrsgm_gb300 as pg
+    prev = pg.set_packed_words(words)
+    try:
+        mine = _runners.run_mine(case)
+    finally:
+        pg.set_packed_words(prev)
+    if _oracle.ref_available():
+        other = _runners.run_ref(case)
+    else:
+        other = _runners.run_oracle(case, _runners.device_lut(case))
+    bad = _runners.compare(mine, other)
+    assert not bad, bad
