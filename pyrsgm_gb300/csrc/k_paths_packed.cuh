@@ -108,11 +108,12 @@ struct Grp {
     static constexpr int LENW = PADW + D + 2;   // words a shifted window can touch
     static constexpr int BUFW = LENW * CPW;     // one window buffer of a warp
     static constexpr int NBUF = T == 1 ? 1 : 2;
-    // Ring slot of a thread: costs [0, NW), partial sums [NW, 2NW), label
-    // base word, image word; strides chosen so that the 16- or 8-byte lane
-    // accesses of a warp hit distinct banks.
+    // Ring slot of a thread: costs [0, NW), partial sums [NW, 2NW); strides
+    // chosen so that the 16- or 8-byte lane accesses of a warp hit distinct
+    // banks.  The label-base and image words of a slot sit in a separate
+    // [slot][2][32] array (bank = lane).
     static constexpr int RSW = NW == 8 ? 20 : (NW == 4 ? 12 : 6);
-    static constexpr int RSW_TB = NW == 2 ? 6 : 12;   // costs, base, image
+    static constexpr int RSW_TB = NW == 8 ? 12 : NW;  // costs only
 };
 
 template <int NW>
@@ -317,13 +318,14 @@ template <int NW, int T>
 constexpr size_t row_smem()
 {
     using G = Grp<NW, T>;
-    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStages * 32 * G::RSW + (G::CPW / 2) * (G::D / 2));
+    return 256 * 4 +
+           (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStages * 32 * (G::RSW + 2) + (G::CPW / 2) * (G::D / 2));
 }
 template <int NW, int T>
 constexpr size_t tb_smem()
 {
     using G = Grp<NW, T>;
-    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStagesTb * 32 * G::RSW_TB);
+    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStagesTb * 32 * (G::RSW_TB + 2));
 }
 
 }  // namespace pk
@@ -342,11 +344,13 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
     int* lut = reinterpret_cast<int*>(smem);
     uint32_t* cbuf = smem + 256;
     uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
+    uint32_t* bibuf = rbuf + kWarps * S * 32 * RS;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
     for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = lane / T, k = lane % T;
+    uint32_t* bi = bibuf + warp * S * 64 + lane;   // [slot][base, image][lane]
     int xlo = 0, xhi = J.w;
     if (!PYR) { xlo = imax(J.minD + D, 0); xhi = J.w + imin(J.minD, 0); }
     const int ncol = xhi - xlo;
@@ -374,8 +378,8 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
         if (yi < H) {
             uint32_t* d = ring + slot * 32 * RS;
             cpw<NW>(d, Cg + oi);
-            if (use_base) cp4(d + NW, word_of(Bg + pi));
-            if (adaptive) cp4(d + NW + 1, word_of(Lg + li));
+            if (use_base) cp4(bi + slot * 64, word_of(Bg + pi));
+            if (adaptive) cp4(bi + slot * 64 + 32, word_of(Lg + li));
         }
         cp_commit();
         ++yi;
@@ -393,13 +397,14 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
         islot = islot + 1 == S ? 0 : islot + 1;
         cp_wait<S - 1>();
         const uint32_t* d = ring + slot * 32 * RS;
+        const uint32_t* db = bi + slot * 64;
         slot = slot + 1 == S ? 0 : slot + 1;
         uint32_t cc[NW];
         ldw<NW>(d, cc);
-        const int base = use_base ? (int)(int16_t)(d[NW] >> ((pc & 1) * 16)) : J.minD;
+        const int base = use_base ? (int)(int16_t)(db[0] >> ((pc & 1) * 16)) : J.minD;
         int p2 = J.P2;
         if (adaptive) {
-            const int img = (int)((d[NW + 1] >> byte_shift(Lg + lc)) & 255u);
+            const int img = (int)((db[32] >> byte_shift(Lg + lc)) & 255u);
             p2 = lut[abs(img - img_prev) & 255];
             img_prev = img;
         }
@@ -428,7 +433,8 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     int* lut = reinterpret_cast<int*>(smem);
     uint32_t* cbuf = smem + 256;
     uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
-    uint32_t* mbuf = rbuf + kWarps * S * 32 * RS;
+    uint32_t* bibuf = rbuf + kWarps * S * 32 * RS;
+    uint32_t* mbuf = bibuf + kWarps * S * 64;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
     for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
     __syncthreads();
@@ -442,6 +448,7 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     const int W = J.w;
     uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
     uint32_t* ring = rbuf + (warp * S * 32 + lane) * RS;
+    uint32_t* bi = bibuf + warp * S * 64 + lane;   // [slot][base, image][lane]
     uint32_t* mid = mbuf + (warp * RPW + r) * (D / 2);
 
     // path extents (single-scale: kernel_AggregateLR/RL ranges)
@@ -495,8 +502,8 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
             uint32_t* d = ring + slot * 32 * RS;
             cpw<NW>(d, Cg + oi);
             if ((ro == 1 && has_tb) || (ro == 2 && !late(ti))) cpw<NW>(d + NW, Vg + oi);
-            if (use_base) cp4(d + 2 * NW, word_of(Bg + pi));
-            if (adaptive) cp4(d + 2 * NW + 1, word_of(Lg + li));
+            if (use_base) cp4(bi + slot * 64, word_of(Bg + pi));
+            if (adaptive) cp4(bi + slot * 64 + 32, word_of(Lg + li));
         }
         cp_commit();
         ++ti;
@@ -519,14 +526,15 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
         cp_wait<S - 1>();
         if (T == 1) __syncwarp();   // orders the other chain's partial sums before the late reads below
         const uint32_t* d = ring + slot * 32 * RS;
+        const uint32_t* db = bi + slot * 64;
         slot = slot + 1 == S ? 0 : slot + 1;
         const int x = xs + dx * t;
         uint32_t cc[NW];
         ldw<NW>(d, cc);
-        const int base = use_base ? (int)(int16_t)(d[2 * NW] >> ((pc & 1) * 16)) : minD;
+        const int base = use_base ? (int)(int16_t)(db[0] >> ((pc & 1) * 16)) : minD;
         int p2 = P2c;
         if (adaptive) {
-            const int img = (int)((d[2 * NW + 1] >> byte_shift(Lg + lc)) & 255u);
+            const int img = (int)((db[32] >> byte_shift(Lg + lc)) & 255u);
             p2 = lut[abs(img - img_prev) & 255];
             img_prev = img;
         }
