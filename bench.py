@@ -491,6 +491,15 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
     outs = {s: outputs_for(*s) for s in shapes}
     # (a) server
     srv = pg.Server(budget, max_batch=max_batch, streams=streams, max_queue=nout - max_batch * streams)
+    # the caller's reused image and output arrays are page-locked once (as the
+    # plain loop below uses pinned buffers)
+    for l, r, _ in pairs_pool:
+        srv.register(l)
+        srv.register(r)
+    for s_outs in outs.values():
+        for o in s_outs:
+            for a in o.values():
+                srv.register(a)
     for k in range(min(4, n)):  # warm the pools
         l, r, c = pairs_pool[picks[k]]
         rid, _ = srv.submit(l, r, params_of(c), outputs=outs[(l.shape[1], l.shape[0])][k])

@@ -165,6 +165,13 @@ void pyrsgm_gb300_server_reset_stats(void* server);
 /* Test hook: the next `batches` batches fail on the host before reaching the
  * GPU, as an allocation failure would; their requests report -1. */
 int pyrsgm_gb300_server_inject_failure(void* server, int batches);
+/* Page-lock a host range (cudaHostRegister): request images and outputs
+ * that lie inside a registered range are copied by DMA in place, the others
+ * through the server's pinned staging with a host memcpy.  0, or -1 with the
+ * reason in err.  Unregister only while no request using it is in flight;
+ * the server unregisters what is left when destroyed. */
+int pyrsgm_gb300_server_register(void* server, void* host, size_t bytes, char* err, size_t err_len);
+int pyrsgm_gb300_server_unregister(void* server, void* host);
 
 /* out[7] = level, width, height, num_labels, max_disparity, block_size, refine */
 int pyrsgm_gb300_matcher_level_info(void* matcher, int level, int* out7);

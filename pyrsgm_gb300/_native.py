@@ -88,6 +88,8 @@ _SIGS = {
     "pyrsgm_gb300_server_stats": (_i, [_vp, C.POINTER(C.c_double)]),
     "pyrsgm_gb300_server_reset_stats": (None, [_vp]),
     "pyrsgm_gb300_server_inject_failure": (_i, [_vp, _i]),
+    "pyrsgm_gb300_server_register": (_i, [_vp, _vp, _sz, C.c_char_p, _sz]),
+    "pyrsgm_gb300_server_unregister": (_i, [_vp, _vp]),
     "pyrsgm_gb300_version": (C.c_char_p, []),
     "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
     "pyrsgm_gb300_set_packed_words": (_i, [_i]),

@@ -267,6 +267,7 @@ class Server:
         if not self._h:
             raise RuntimeError(err.value.decode())
         self._keep: dict[int, tuple] = {}
+        self._reg: dict[int, object] = {}
 
     def submit(self, left, right, params: Params, want16: bool = True, want32: bool = False,
                want_conf: bool = False, outputs: dict | None = None):
@@ -315,10 +316,24 @@ class Server:
     def inject_failure(self, batches: int) -> None:
         lib().pyrsgm_gb300_server_inject_failure(self._h, batches)
 
+    def register(self, arr) -> bool:
+        """Page-lock a numpy array the caller reuses for images or outputs, so
+        that requests using it skip the staging copies.  False if refused."""
+        err = C.create_string_buffer(256)
+        ok = lib().pyrsgm_gb300_server_register(self._h, arr.ctypes.data, arr.nbytes, err, 256) == 0
+        if ok:
+            self._reg[arr.ctypes.data] = arr
+        return ok
+
+    def unregister(self, arr) -> None:
+        if self._reg.pop(arr.ctypes.data, None) is not None:
+            lib().pyrsgm_gb300_server_unregister(self._h, arr.ctypes.data)
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib().pyrsgm_gb300_server_destroy(self._h)
             self._h = None
+            self._reg = {}
 
     __del__ = close
 

@@ -11,6 +11,10 @@
 // waits for each lane's event in order, hands the results to the callers'
 // buffers and records the latency (submit -> results in host memory).
 //
+// Host buffers that the caller registered (pyrsgm_gb300_server_register,
+// page-locked with cudaHostRegister) are copied by DMA directly; other
+// buffers go through the lane's pinned staging with a host memcpy.
+//
 // Device memory stays resident: each lane keeps its batch engine's pooled
 // pair plans and a pool of input/output buffers per image size.  A request
 // is admitted only if it fits a lane's budget on its own; a batch is cut
@@ -113,6 +117,7 @@ struct Lane {
     std::map<std::pair<int, int>, std::vector<std::unique_ptr<IOBuf>>> pool;
     std::vector<Request*> reqs;
     std::vector<IOBuf*> bufs;
+    std::vector<void*> staged;   // per request and output: staging used (null: copied in place or absent)
     bool busy = false;
     std::string error;  // set when the batch failed before reaching the GPU
 };
@@ -153,6 +158,7 @@ public:
             cudaEventDestroy(L->done);
             cudaStreamDestroy(L->st);
         }
+        for (auto& kv : reg_) cudaHostUnregister(reinterpret_cast<void*>(kv.first));
     }
 
     long long submit(const pyrsgm_gb300_request& r, std::string& err)
@@ -257,6 +263,37 @@ public:
         inject_ += n;
     }
 
+    // Page-lock a host range so that requests whose images or outputs lie
+    // inside it are copied without staging.
+    int register_host(void* p, size_t bytes, std::string& err)
+    {
+        if (!p || bytes == 0) {
+            err = "null or empty range";
+            return -1;
+        }
+        const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            err = cudaGetErrorString(e);
+            return -1;
+        }
+        std::lock_guard<std::mutex> lk(reg_mu_);
+        reg_[reinterpret_cast<uintptr_t>(p)] = bytes;
+        return 0;
+    }
+
+    // Only between requests that use the range (none in flight).
+    int unregister_host(void* p)
+    {
+        {
+            std::lock_guard<std::mutex> lk(reg_mu_);
+            auto it = reg_.find(reinterpret_cast<uintptr_t>(p));
+            if (it == reg_.end()) return -1;
+            reg_.erase(it);
+        }
+        return cudaHostUnregister(p) == cudaSuccess ? 0 : -1;
+    }
+
 private:
     static pyrsgm::Params toParams(const pyrsgm_gb300_params& c)
     {
@@ -283,6 +320,16 @@ private:
         p.p2_lower_mult = c.p2_lower_mult;
         p.p2_upper_mult = c.p2_upper_mult;
         return p;
+    }
+
+    bool registered(const void* p, size_t bytes)
+    {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+        std::lock_guard<std::mutex> lk(reg_mu_);
+        auto it = reg_.upper_bound(a);
+        if (it == reg_.begin()) return false;
+        --it;
+        return a >= it->first && a + bytes <= it->first + it->second;
     }
 
     IOBuf* take_buf(Lane& L, int w, int h, std::map<std::pair<int, int>, int>& used)
@@ -334,6 +381,7 @@ private:
             }
             L->reqs = batch;
             L->bufs.clear();
+            L->staged.clear();
             L->error.clear();
             try {
                 if (fail_batch) throw std::runtime_error("injected allocation failure");
@@ -360,10 +408,18 @@ private:
             IOBuf* b = take_buf(L, r.width, r.height, used);
             L.bufs.push_back(b);
             const size_t px = (size_t)r.width * r.height;
-            std::memcpy(b->hL, r.h_left, px);
-            std::memcpy(b->hR, r.h_right, px);
-            if (cudaMemcpyAsync(b->dL, b->hL, px, cudaMemcpyHostToDevice, L.st) != cudaSuccess ||
-                cudaMemcpyAsync(b->dR, b->hR, px, cudaMemcpyHostToDevice, L.st) != cudaSuccess)
+            const void* srcL = r.h_left;
+            const void* srcR = r.h_right;
+            if (!registered(srcL, px)) {
+                std::memcpy(b->hL, r.h_left, px);
+                srcL = b->hL;
+            }
+            if (!registered(srcR, px)) {
+                std::memcpy(b->hR, r.h_right, px);
+                srcR = b->hR;
+            }
+            if (cudaMemcpyAsync(b->dL, srcL, px, cudaMemcpyHostToDevice, L.st) != cudaSuccess ||
+                cudaMemcpyAsync(b->dR, srcR, px, cudaMemcpyHostToDevice, L.st) != cudaSuccess)
                 throw std::runtime_error("input copy failed");
             pyrsgm_gb300_pair p{};
             p.d_left = b->dL;
@@ -386,9 +442,19 @@ private:
             const pyrsgm_gb300_request& r = L.reqs[i]->r;
             IOBuf* b = L.bufs[i];
             const size_t px = (size_t)r.width * r.height;
-            if (r.h_disp16) cudaMemcpyAsync(b->h16, b->d16, px * 2, cudaMemcpyDeviceToHost, L.st);
-            if (r.h_disp32) cudaMemcpyAsync(b->h32, b->d32, px * 4, cudaMemcpyDeviceToHost, L.st);
-            if (r.h_conf) cudaMemcpyAsync(b->hc, b->dc, px * 4, cudaMemcpyDeviceToHost, L.st);
+            // outputs in registered memory land in place; the others in staging
+            auto out = [&](void* user, void* stage, const void* dev, size_t n) {
+                if (!user) {
+                    L.staged.push_back(nullptr);
+                    return;
+                }
+                const bool direct = registered(user, n);
+                cudaMemcpyAsync(direct ? user : stage, dev, n, cudaMemcpyDeviceToHost, L.st);
+                L.staged.push_back(direct ? nullptr : stage);
+            };
+            out(r.h_disp16, b->h16, b->d16, px * 2);
+            out(r.h_disp32, b->h32, b->d32, px * 4);
+            out(r.h_conf, b->hc, b->dc, px * 4);
         }
     }
 
@@ -415,9 +481,10 @@ private:
                 const pyrsgm_gb300_request& r = L->reqs[i]->r;
                 IOBuf* b = L->bufs[i];
                 const size_t px = (size_t)r.width * r.height;
-                if (r.h_disp16) std::memcpy(r.h_disp16, b->h16, px * 2);
-                if (r.h_disp32) std::memcpy(r.h_disp32, b->h32, px * 4);
-                if (r.h_conf) std::memcpy(r.h_conf, b->hc, px * 4);
+                const void* const* st = &L->staged[3 * i];
+                if (r.h_disp16 && st[0]) std::memcpy(r.h_disp16, b->h16, px * 2);
+                if (r.h_disp32 && st[1]) std::memcpy(r.h_disp32, b->h32, px * 4);
+                if (r.h_conf && st[2]) std::memcpy(r.h_conf, b->hc, px * 4);
             }
             const double t = now_s();
             {
@@ -445,6 +512,8 @@ private:
     }
 
     const int max_batch_, max_queue_;
+    std::mutex reg_mu_;
+    std::map<uintptr_t, size_t> reg_;   // registered host ranges: start -> bytes
     size_t lane_budget_ = 0;
     std::vector<std::unique_ptr<Lane>> lanes_;
     std::mutex mu_;
@@ -526,6 +595,23 @@ int pyrsgm_gb300_server_inject_failure(void* s, int batches)
     if (!s) return -1;
     static_cast<pg::Server*>(s)->inject_failure(batches);
     return 0;
+}
+
+int pyrsgm_gb300_server_register(void* s, void* host, size_t bytes, char* err, size_t err_len)
+{
+    if (!s) {
+        setErr(err, err_len, "null server");
+        return -1;
+    }
+    std::string e;
+    const int r = static_cast<pg::Server*>(s)->register_host(host, bytes, e);
+    if (r != 0) setErr(err, err_len, e);
+    return r;
+}
+
+int pyrsgm_gb300_server_unregister(void* s, void* host)
+{
+    return s ? static_cast<pg::Server*>(s)->unregister_host(host) : -1;
 }
 
 }  // extern "C"

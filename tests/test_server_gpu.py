@@ -120,3 +120,31 @@ def test_full_queue_refuses():
     for rid in ids:
         assert srv.wait(rid, 60.0) == 1
     srv.close()
+
+
+def test_registered_buffers_are_copied_in_place():
+    """Images and outputs the caller registered (page-locked) skip the staging
+    copies; results equal those of the pair alone, also when only some of a
+    request's buffers are registered."""
+    reqs = _requests(8, seed=6100)
+    srv = pg.Server(2 << 30, max_batch=4, streams=2)
+    subs = []
+    for i, (p, left, right) in enumerate(reqs):
+        h, w = left.shape
+        left = np.ascontiguousarray(left)
+        right = np.ascontiguousarray(right)
+        out = {"disp16": np.empty((h, w), np.int16), "disp32": np.empty((h, w), np.float32),
+               "conf": np.empty((h, w), np.float32)}
+        regs = [left, right] + list(out.values())
+        for j, a in enumerate(regs):
+            if (i + j) % 3 != 0:  # leave some buffers to the staging path
+                srv.register(a)
+        rid, _ = srv.submit(left, right, p, outputs=out)
+        subs.append((rid, p, left, right, out))
+    for rid, p, left, right, out in subs:
+        assert srv.wait(rid) == 1, getattr(srv, "last_error", "")
+        ref = _alone(p, left, right)
+        np.testing.assert_array_equal(out["disp16"], ref["disp16"])
+        np.testing.assert_allclose(out["disp32"], ref["disp32"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(out["conf"], ref["conf"], atol=1e-6, rtol=0)
+    srv.close()
