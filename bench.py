@@ -52,6 +52,12 @@ def params_for(cost: int) -> dict:
                 pyramid_coarse_disparities=128)
 
 
+# DRAM bytes per algorithmic byte of k_grow, from one ncu capture of its
+# level-0 launch for four 1080p pairs (dram read + write 1.460 GB against
+# 1.112 GB algorithmic); the partial sums of the meeting scheme are the extra.
+K_GROW_TRAFFIC_PER_ALG_BYTE = 1.314
+
+
 def peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -644,13 +650,18 @@ def run(args) -> dict | None:
         out["roofline"] = {"kernel": "k_grow (L->R + R->L path sums, three-path totals)", "bound": "hbm",
                            "achieved": round(achieved, 2) if achieved else None, "peak": pk["hbm_gbs"],
                            "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4) if achieved else None,
-                           "peak_source": pk["source"], "traffic": None,
+                           "peak_source": pk["source"],
+                           "traffic": round(K_GROW_TRAFFIC_PER_ALG_BYTE * row["bytes"] / row["launches"] / 1e9, 4)
+                           if row.get("launches") else None,
+                           "traffic_unit": "GB per launch (ncu capture scaled by voxels)",
                            "avg_launch_ms": round(row["ms"] / row["launches"], 5) if row.get("launches") else None}
         out["kernels_ms_per_step"] = {k: round(v["ms"] / headline["prof_steps"], 4)
                                       for k, v in prof.items() if v["launches"]}
     else:
         out["impl"] = "reference"
         out["reference_build"] = "reference src/sgm_kernels.cu + src/pyrdown.cu compiled unmodified for sm_103a"
+    if args.impl == "mine" and world == 1:
+        out["latency_1080p_d256_l2_census"] = single_pair_latency(dev, stream)
     if args.impl == "mine" and world == 1 and args.serve_requests > 0:
         import pyrsgm_gb300 as pg
         rate = round(0.7 * value, 1)
@@ -658,6 +669,35 @@ def run(args) -> dict | None:
     if not args.no_cpu and world == 1:
         out["cpu_baseline"] = cpu_baseline(pairs)
     return out
+
+
+def single_pair_latency(dev, stream, runs: int = 20) -> dict:
+    """One 1920x1080 D=256 pyramid_levels=2 Census pair through plain
+    compute() (disp16 + disp32 + conf), device-resident, per-call CUDA
+    events; p50/p99 over `runs` calls after 3 warm-ups."""
+    import torch
+    import pyrsgm_gb300 as pg
+    from pyrsgm_gb300 import synth
+    p = pg.Params(**{**params_for(CENSUS), "pyramid_levels": 2})
+    left, right, _ = synth.make_pair(W, H, D - 1, 16, 7000)
+    m = pg.StereoMatcher(W, H, p)
+    L, R = torch.from_numpy(left).to(dev), torch.from_numpy(right).to(dev)
+    d16 = torch.empty((H, W), dtype=torch.int16, device=dev)
+    d32 = torch.empty((H, W), dtype=torch.float32, device=dev)
+    cf = torch.empty((H, W), dtype=torch.float32, device=dev)
+    ms = []
+    for k in range(3 + runs):
+        with torch.cuda.stream(stream):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            m.compute_into(L, R, d16, d32, cf, stream)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if k >= 3:
+            ms.append(a.elapsed_time(b))
+    m.close()
+    return {"p50_ms": round(_pct(ms, 0.5), 4), "p99_ms": round(_pct(ms, 0.99), 4), "runs": runs,
+            "levels": [(li.width, li.height, li.num_labels) for li in pg.level_geometry(W, H, p)]}
 
 
 MIX_SIZES = [(640, 480), (960, 540), (1280, 720), (1920, 1080)]
