@@ -52,7 +52,7 @@ static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 size_t Workspace::bytes_for(int w, int h, int D)
 {
     const size_t px = (size_t)w * h;
-    return align256(px * 8) * 2 + align256(px * 2) + align256(px * D * 2) * 2 + align256(px * 2) +
+    return align256(px * 16) * 2 + align256(px * 2) + align256(px * D * 2) * 2 + align256(px * 2) +
            align256(px * 4) * 2 + align256(256 * 4);
 }
 
@@ -75,8 +75,8 @@ int Workspace::ensure(int w, int h, int D)
 void Workspace::carve(unsigned char* p, int w, int h, int D)
 {
     const size_t px = (size_t)w * h;
-    featL = reinterpret_cast<uint2*>(p); p += align256(px * 8);
-    featR = reinterpret_cast<uint2*>(p); p += align256(px * 8);
+    featL = reinterpret_cast<uint4*>(p); p += align256(px * 16);
+    featR = reinterpret_cast<uint4*>(p); p += align256(px * 16);
     base = reinterpret_cast<int16_t*>(p); p += align256(px * 2);
     C = reinterpret_cast<int16_t*>(p); p += align256(px * D * 2);
     V = reinterpret_cast<int16_t*>(p); p += align256(px * D * 2);

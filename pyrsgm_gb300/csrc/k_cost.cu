@@ -8,6 +8,8 @@
 
 namespace pg {
 
+constexpr uint32_t kBtBias2 = 0x01000100u;   // 256 in each 16-bit half
+
 // ---------------------------------------------------------------------------
 // pyrDown: 5x5 [1 4 6 4 1]^2 / 256, BORDER_REFLECT_101, (sum+128)>>8.
 // Reference: src/pyrdown.cu:16-52.  One block computes a 32x8 output tile
@@ -59,8 +61,10 @@ __global__ void __launch_bounds__(256) k_pyrdown(const __grid_constant__ PyrDown
 // x-gradient clipped to +-ftzero and offset by ftzero
 // (src/sgm_kernels.cu:94-118), plus for both the gradient and intensity
 // channels the half-sample interval [lo, hi] of dev_bt_channel_cost
-// (src/sgm_kernels.cu:1002-1028) with clamped neighbours, packed as
-// v | lo<<8 | hi<<16.
+// (src/sgm_kernels.cu:1002-1028) with clamped neighbours.  Census pixels
+// store their 25-bit descriptor as one word per pixel; BT pixels store four
+// words of 16-bit pairs (gradient low half, intensity high half):
+// value + 256, value, lo + 256, hi — the operands of bt_pixel().
 // ---------------------------------------------------------------------------
 constexpr int kFtX = 32, kFtY = 8, kFtHalo = 2;
 constexpr int kFtW = kFtX + 2 * kFtHalo, kFtH = kFtY + 2 * kFtHalo;
@@ -74,7 +78,7 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
     if (x0 >= J.w || y0 >= J.h) return;
     const uint8_t* img = view ? J.right : J.left;
     const int step = view ? J.rstep : J.lstep;
-    uint2* feat = view ? J.featR : J.featL;
+    uint4* feat = view ? J.featR : J.featL;
     const int W = J.w, H = J.h;
 
     __shared__ uint8_t t[kFtH][kFtW];
@@ -88,7 +92,7 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
     if (x >= W || y >= H) return;
     // pixel (gy, gx), both already clamped to the image
     auto px = [&](int gy, int gx) -> int { return t[gy - y0 + kFtHalo][gx - x0 + kFtHalo]; };
-    uint2 f;
+    const size_t p = (size_t)y * W + x;
     if (J.cost == COST_CENSUS) {
         const int c = px(y, x);
         uint32_t cv = 0;
@@ -101,7 +105,7 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
                 cv |= (uint32_t)(px(gy, iclamp(x + dx - 2, 0, W - 1)) < c);
             }
         }
-        f = make_uint2(cv, 0u);
+        reinterpret_cast<uint32_t*>(feat)[p] = cv;
     } else {
         const int ftzero = imax(J.pfc, 15) | 1;
         const int yp = imax(y - 1, 0), yn = imin(y + 1, H - 1);
@@ -112,17 +116,21 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
             g += px(yn, xn) - px(yn, xp);
             return iclamp(g, -ftzero, ftzero) + ftzero;
         };
-        auto interval = [](int v, int l, int r) -> uint32_t {
+        // value, lo, hi of one channel as 16-bit fields
+        auto interval = [](int v, int l, int r, uint32_t& lo, uint32_t& hi) {
             const int vl = (v + l) / 2, vr = (v + r) / 2;
-            const int lo = imin(imin(vl, vr), v), hi = imax(imax(vl, vr), v);
-            return (uint32_t)v | ((uint32_t)lo << 8) | ((uint32_t)hi << 16);
+            lo = (uint32_t)imin(imin(vl, vr), v);
+            hi = (uint32_t)imax(imax(vl, vr), v);
         };
         const int xm = imax(x - 1, 0), xq = imin(x + 1, W - 1);
-        f.x = interval(grad(x), grad(xm), grad(xq));
-        f.y = interval(px(y, x), px(y, xm), px(y, xq));
+        const int gv = grad(x), iv = px(y, x);
+        uint32_t glo, ghi, ilo, ihi;
+        interval(gv, grad(xm), grad(xq), glo, ghi);
+        interval(iv, px(y, xm), px(y, xq), ilo, ihi);
+        const uint32_t X = (uint32_t)gv | ((uint32_t)iv << 16), X0 = glo | (ilo << 16), X1 = ghi | (ihi << 16);
+        feat[p] = make_uint4(X + kBtBias2, X, X0 + kBtBias2, X1);
     }
-    feat[(size_t)y * W + x] = f;
-    if (view == 0) J.keys[(size_t)y * W + x] = 0xffffffffu;  // no disp2 candidate yet
+    if (view == 0) J.keys[p] = 0xffffffffu;  // no disp2 candidate yet
 }
 
 // ---------------------------------------------------------------------------
@@ -197,8 +205,8 @@ __global__ void __launch_bounds__(256) k_cost_census(const __grid_constant__ Job
     if (x >= J.w || y >= J.h) return;
     const int W = J.w, D = J.D;
     const size_t p = (size_t)y * W + x;
-    const uint32_t cl = J.featL[p].x;
-    const uint2* rrow = J.featR + (size_t)y * W;
+    const uint32_t cl = reinterpret_cast<const uint32_t*>(J.featL)[p];
+    const uint32_t* rrow = reinterpret_cast<const uint32_t*>(J.featR) + (size_t)y * W;
     // label d reads right pixel x - off - d when lo <= d <= hi, else `fill`
     int off, lo, hi, fill;
     if (J.refine) {
@@ -212,7 +220,7 @@ __global__ void __launch_bounds__(256) k_cost_census(const __grid_constant__ Job
         fill = 24;
     }
     auto cost = [&](int d) -> uint32_t {
-        return (d >= lo && d <= hi) ? (uint32_t)__popc(cl ^ __ldg(&rrow[x - off - d].x)) : (uint32_t)fill;
+        return (d >= lo && d <= hi) ? (uint32_t)__popc(cl ^ __ldg(&rrow[x - off - d])) : (uint32_t)fill;
     };
     int16_t* out = J.C + p * D;
     if ((D & 7) == 0) {
@@ -227,20 +235,18 @@ __global__ void __launch_bounds__(256) k_cost_census(const __grid_constant__ Job
     }
 }
 
-// BT cost of one (left pixel, right pixel) pair from packed features:
-// dev_bt_pixel_cost, src/sgm_kernels.cu:1030-1043.
-__device__ __forceinline__ int bt_channel(uint32_t a, uint32_t b)
+// BT cost of one (left pixel, right pixel) pair: dev_bt_pixel_cost,
+// src/sgm_kernels.cu:1030-1043, i.e. min(255, bt(gradient) + bt(intensity)
+// >> 2) with bt(u, v) = min(max(0, u - v.hi, v.lo - u), max(0, v - u.hi,
+// u.lo - v)), on both channels at once as 16-bit pairs.  The +256 bias in
+// the features keeps every difference positive (no borrow between halves)
+// and is the floor of the maxima, subtracted once at the end.
+__device__ __forceinline__ int bt_pixel(const uint4 l, const uint4 r)
 {
-    const int u = a & 255, u0 = (a >> 8) & 255, u1 = (a >> 16) & 255;
-    const int v = b & 255, v0 = (b >> 8) & 255, v1 = (b >> 16) & 255;
-    const int c0 = imax(imax(0, u - v1), v0 - u);
-    const int c1 = imax(imax(0, v - u1), u0 - v);
-    return imin(c0, c1);
-}
-
-__device__ __forceinline__ int bt_pixel(uint2 l, uint2 r)
-{
-    return imin(255, bt_channel(l.x, r.x) + (bt_channel(l.y, r.y) >> 2));
+    const uint32_t c0 = __vimax3_u16x2(kBtBias2, l.x - r.w, r.z - l.y);   // 256 + max(0, u - v.hi, v.lo - u)
+    const uint32_t c1 = __vimax3_u16x2(kBtBias2, r.x - l.w, l.z - r.y);   // 256 + max(0, v - u.hi, u.lo - v)
+    const uint32_t t = __vminu2(c0, c1) - kBtBias2;
+    return imin(255, (int)(t & 0xffffu) + (int)(t >> 18));
 }
 
 // ---------------------------------------------------------------------------
@@ -333,8 +339,8 @@ __device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, in
                                             int r0, int rn, int lane)
 {
     const int W = J.w;
-    const uint2* lrow = J.featL + (size_t)gy * W;
-    const uint2* rrow = J.featR + (size_t)gy * W;
+    const uint4* lrow = J.featL + (size_t)gy * W;
+    const uint4* rrow = J.featR + (size_t)gy * W;
     const int ri = r0 + lane;
     const int real = rmin + ri;
     int q[2 * HW + 1];   // q[0 .. 2HW-1]: the last 2HW costs, oldest first
@@ -434,11 +440,11 @@ __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ J
         if (b != kNoParent) {
             for (int dy = -h; dy <= h; ++dy) {
                 const int gy = iclamp(y + dy, 0, H - 1);
-                const uint2* lrow = J.featL + (size_t)gy * W;
-                const uint2* rrow = J.featR + (size_t)gy * W;
+                const uint4* lrow = J.featL + (size_t)gy * W;
+                const uint4* rrow = J.featR + (size_t)gy * W;
                 for (int dx = -h; dx <= h; ++dx) {
                     const int gx = iclamp(x + dx, 0, W - 1);
-                    const uint2 lf = __ldg(&lrow[gx]);
+                    const uint4 lf = __ldg(&lrow[gx]);
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const int x2 = gx - (b + d0 + i);
@@ -500,7 +506,7 @@ cudaError_t launch_prepare(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStrea
     prof_begin(st);
     k_features<NJ><<<gf, 256, 0, st>>>(jobs);
     count_launch();
-    prof_end(PK_FEATURES, jobs_px(jobs) * 2 * (1 + 8), st);  // read u8, write uint2, both views
+    prof_end(PK_FEATURES, jobs_px(jobs) * 2 * (1 + (jobs.d[0].cost == COST_CENSUS ? 4 : 16)), st);  // read u8, write features, both views
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     if (e.any_refine) {
@@ -545,7 +551,7 @@ cudaError_t launch_cost(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t
     }
     count_launch();
     // write the int16 volume, read both views' features (and the label base)
-    prof_end(PK_COST, jobs_vox(jobs) * 2 + jobs_px(jobs) * (16 + (J0.refine ? 2 : 0)), st);
+    prof_end(PK_COST, jobs_vox(jobs) * 2 + jobs_px(jobs) * ((J0.cost == COST_CENSUS ? 8 : 32) + (J0.refine ? 2 : 0)), st);
     return cudaGetLastError();
 }
 

@@ -3,9 +3,10 @@
 //
 // Layout in HBM (one level of one stereo pair):
 //   images            u8, caller-pitched (bytes)
-//   features          uint2 per pixel and view: census bits (.x) for the
-//                     Census cost, or the Birchfield-Tomasi sample intervals
-//                     of the gradient (.x) and intensity (.y) channels
+//   features          16 bytes per pixel and view: the census descriptor
+//                     (one word per pixel, dense) for the Census cost, or
+//                     the Birchfield-Tomasi operands (value + 256, value,
+//                     lo + 256, hi; gradient and intensity as 16-bit pairs)
 //   label base        int16 per pixel (refine levels); kNoParent marks pixels
 //                     whose parent was rejected (no valid label)
 //   cost volume C     int16 [y][x][D], d innermost
@@ -34,8 +35,8 @@ struct LevelDesc {
     const int16_t* pdisp;
     const float* pconf;
     // workspace (device)
-    uint2* featL;
-    uint2* featR;
+    uint4* featL;
+    uint4* featR;
     int16_t* base;
     int16_t* C;
     int16_t* V;

@@ -1,6 +1,6 @@
 // workspace.h -- device buffers of one level geometry (the opaque object
 // behind pyrsgm_create_workspace).  One cudaMalloc, carved into:
-//   featL, featR  uint2  [h][w]     census bits or BT sample intervals
+//   featL, featR  uint4  [h][w]     census descriptors (dense words) or BT operands
 //   base          int16  [h][w]     refine label base (kNoParent = rejected)
 //   C             int16  [h][w][D]  matching cost
 //   V             int16  [h][w][D]  aggregation volume
@@ -25,8 +25,8 @@ struct Workspace {
     size_t bytes = 0;
     bool owned = false;
     int debug = 0;
-    uint2* featL = nullptr;
-    uint2* featR = nullptr;
+    uint4* featL = nullptr;
+    uint4* featR = nullptr;
     int16_t* base = nullptr;
     int16_t* C = nullptr;
     int16_t* V = nullptr;
