@@ -49,6 +49,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "profiler.h"
 #include "sgm_common.cuh"
@@ -496,12 +497,21 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     size_t oi = (prow + xs) * D + 2 * NW * k, pi = prow + xs, li = lrow + xs;
     size_t oc = oi, pc = pi, lc = li;
     int ti = 0;
-    auto issue_next = [&](int slot) {
-        if (ti < n_mine) {
-            const int ro = role(ti);
+    // MODE 0: role per step; 1: every chain of the warp is first, not late;
+    // 2: every chain is second, not late (see the loop split below)
+    auto issue_next = [&](int slot, auto mode) {
+        constexpr int MODE = decltype(mode)::value;
+        if (MODE == 1 || ti < n_mine) {
             uint32_t* d = ring + slot * 32 * RS;
             cpw<NW>(d, Cg + oi);
-            if ((ro == 1 && has_tb) || (ro == 2 && !late(ti))) cpw<NW>(d + NW, Vg + oi);
+            if (MODE == 1) {
+                if (has_tb) cpw<NW>(d + NW, Vg + oi);
+            } else if (MODE == 2) {
+                cpw<NW>(d + NW, Vg + oi);
+            } else {
+                const int ro = role(ti);
+                if ((ro == 1 && has_tb) || (ro == 2 && !late(ti))) cpw<NW>(d + NW, Vg + oi);
+            }
             if (use_base) cp4(bi + slot * 64, word_of(Bg + pi));
             if (adaptive) cp4(bi + slot * 64 + 32, word_of(Lg + li));
         }
@@ -516,12 +526,13 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     GChain<NW> s;
     gchain_init(s, minD);
 #pragma unroll
-    for (int j = 0; j < S - 1; ++j) issue_next(j);
+    for (int j = 0; j < S - 1; ++j) issue_next(j, std::integral_constant<int, 0>{});
     int img_prev = 0, slot = 0, islot = S - 1;
     bool defer = false;
     int xm = 0;
-    for (int t = 0; t < Tn; ++t) {
-        issue_next(islot);
+    auto step = [&](int t, auto mode) {
+        constexpr int MODE = decltype(mode)::value;
+        issue_next(islot, mode);
         islot = islot + 1 == S ? 0 : islot + 1;
         cp_wait<S - 1>();
         if (T == 1) __syncwarp();   // orders the other chain's partial sums before the late reads below
@@ -545,8 +556,8 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
         }
         uint32_t* cw = chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0);
         gstep<NW, T, PYR>(s, cc, base, p2, p12, cw, k);
-        const int ro = role(t);
         uint32_t* vp = reinterpret_cast<uint32_t*>(Vg + oc);
+        const int ro = MODE == 0 ? role(t) : MODE;
         if (ro == 1) {
             uint32_t part[NW];
             if (has_tb) {
@@ -559,24 +570,39 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
                 for (int i = 0; i < NW; ++i) part[i] = s.L[i];
             }
             if (row_ok) stw<NW>(vp, part);
-        } else if (ro == 4) {
-            stw<NW>(mid + NW * k, s.L);
-            defer = true;
-            xm = x;
         } else if (ro == 2) {
             uint32_t part[NW], tot[NW];
-            if (late(t)) ldw<NW>(vp, part);
+            if (MODE == 0 && late(t)) ldw<NW>(vp, part);
             else ldw<NW>(d + NW, part);
 #pragma unroll
             for (int i = 0; i < NW; ++i) tot[i] = gcombine<PYR>(part[i], s.L[i]);
             if (row_ok) stw<NW>(vp, tot);
+        } else if (ro == 4) {
+            stw<NW>(mid + NW * k, s.L);
+            defer = true;
+            xm = x;
         } else if (ro == 3) {
             if (row_ok) stw<NW>(vp, s.L);
         }
         oc += dxD;
         pc += dx;
         lc += dx;
+    };
+    // Steps [ta, tb): all chains first and their loads S - 1 steps ahead too;
+    // [tc, td): all chains second, past the late zone; the rest per step.
+    int ta = 0, tb = 0, tc = 0, td = 0;
+    if (has_lr) {
+        ta = W - lr_x0 - lr_n;                                   // R->L reaches the L->R range
+        tb = imax(ta, imin((M - S - 1 + 1) / 2, lr_n) - (S - 1)); // before the late zone, loads included
+        tc = imax(tb, (M + S + 1) / 2 + 1);                       // after the late zone
+        td = imax(tc, imin(lr_n, rl_n));
     }
+    int t = 0;
+    for (; t < ta; ++t) step(t, std::integral_constant<int, 0>{});
+    for (; t < tb; ++t) step(t, std::integral_constant<int, 1>{});
+    for (; t < tc; ++t) step(t, std::integral_constant<int, 0>{});
+    for (; t < td; ++t) step(t, std::integral_constant<int, 2>{});
+    for (; t < Tn; ++t) step(t, std::integral_constant<int, 0>{});
     cp_wait<0>();
     __syncwarp();
     if (defer && row_ok) {
