@@ -330,29 +330,46 @@ __global__ void __launch_bounds__(256) k_cost_bt_box(const __grid_constant__ Job
 // ---------------------------------------------------------------------------
 constexpr int kTiX = 32, kTiY = 8, kTiRn = 64, kTiMaxHalf = 2;
 constexpr int kTiRs = kTiRn + 2;   // halves per (row, column): 33 words, odd, so columns hit distinct banks
-constexpr size_t kTiSmem = (size_t)(kTiY + 2 * kTiMaxHalf) * kTiX * kTiRs * 2;
+constexpr int kTiStage = 2 * (kTiX + 2 * kTiMaxHalf) + 32;   // staged left (SW) + right (SW + 31) features of a row unit
+constexpr size_t kTiHs = (size_t)(kTiY + 2 * kTiMaxHalf) * kTiX * kTiRs * 2;
+constexpr size_t kTiSmem = kTiHs + (size_t)kTiY * kTiStage * 16;
 
 // Sums along x of one window row r (image row gy) for the 32 real
 // disparities rmin + r0 + lane: a running sum over the last 2*HW+1 costs.
+// The row's left features (one per window column) and the right features
+// the 32 lanes reach are first staged in the warp's shared buffer `st`.
 template <int HW>
-__device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, int r, int gy, int x0, int rmin,
-                                            int r0, int rn, int lane)
+__device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, uint4* st, int r, int gy, int x0,
+                                            int rmin, int r0, int rn, int lane)
 {
+    constexpr int SW = kTiX + 2 * HW;
     const int W = J.w;
     const uint4* lrow = J.featL + (size_t)gy * W;
     const uint4* rrow = J.featR + (size_t)gy * W;
+    // right pixels gx - real for gx in [x0 - HW, x0 + 31 + HW], real in [rmin + r0, rmin + r0 + 31]
+    const int xr0 = x0 - HW - (rmin + r0 + 31);
+    uint4* sl = st;            // [SW] left, clamped columns
+    uint4* sr = st + SW;       // [SW + 31] right, from xr0
+    for (int i = lane; i < SW; i += 32) sl[i] = __ldg(&lrow[iclamp(x0 - HW + i, 0, W - 1)]);
+    for (int i = lane; i < SW + 31; i += 32) {
+        const int xx = xr0 + i;
+        if (xx >= 0 && xx < W) sr[i] = __ldg(&rrow[xx]);
+    }
+    __syncwarp();
     const int ri = r0 + lane;
     const int real = rmin + ri;
     int q[2 * HW + 1];   // q[0 .. 2HW-1]: the last 2HW costs, oldest first
 #pragma unroll
     for (int i = 0; i < 2 * HW + 1; ++i) q[i] = 0;
     int s = 0;
-    for (int j = 0; j < kTiX + 2 * HW; ++j) {
+    uint16_t* out = hs + (size_t)r * kTiX * kTiRs + ri;
+#pragma unroll 4
+    for (int j = 0; j < SW; ++j) {
         const int gx = iclamp(x0 - HW + j, 0, W - 1);
         const int x2 = gx - real;
-        const int e = (x2 >= 0 && x2 < W) ? bt_pixel(__ldg(&lrow[gx]), __ldg(&rrow[x2])) : 255;
+        const int e = (x2 >= 0 && x2 < W) ? bt_pixel(sl[j], sr[x2 - xr0]) : 255;
         s += e;
-        if (j >= 2 * HW && ri < rn) hs[(r * kTiX + j - 2 * HW) * kTiRs + ri] = (uint16_t)s;
+        if (j >= 2 * HW && ri < rn) out[(j - 2 * HW) * kTiRs] = (uint16_t)s;
         if (HW > 0) {
             s -= q[0];
 #pragma unroll
@@ -362,6 +379,7 @@ __device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, in
             s = 0;
         }
     }
+    __syncwarp();   // the staging buffer is refilled by the warp's next unit
 }
 
 template <int NJ>
@@ -371,7 +389,8 @@ __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ J
     const int x0 = blockIdx.x * kTiX, y0 = blockIdx.y * kTiY;
     if (x0 >= J.w || y0 >= J.h) return;
     const int W = J.w, H = J.h, D = J.D, h = J.bs / 2;
-    extern __shared__ __align__(16) uint16_t hs[];   // [kTiY + 2h][kTiX][kTiRs]
+    extern __shared__ __align__(16) uint16_t hs[];   // [kTiY + 2h][kTiX][kTiRs], then per warp kTiStage uint4
+    uint4* stg = reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(hs) + kTiHs) + (threadIdx.x >> 5) * kTiStage;
     __shared__ int wred[2][kTiY];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int x = x0 + lane, y = y0 + warp;
@@ -394,9 +413,9 @@ __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ J
         for (int u = warp; u < (kTiY + 2 * h) * nch; u += kTiY) {
             const int r = u / nch, r0 = (u - r * nch) * 32;
             const int gy = iclamp(y0 - h + r, 0, H - 1);
-            if (h == 2) bt_row_sums<2>(J, hs, r, gy, x0, rmin, r0, rn, lane);
-            else if (h == 1) bt_row_sums<1>(J, hs, r, gy, x0, rmin, r0, rn, lane);
-            else bt_row_sums<0>(J, hs, r, gy, x0, rmin, r0, rn, lane);
+            if (h == 2) bt_row_sums<2>(J, hs, stg, r, gy, x0, rmin, r0, rn, lane);
+            else if (h == 1) bt_row_sums<1>(J, hs, stg, r, gy, x0, rmin, r0, rn, lane);
+            else bt_row_sums<0>(J, hs, stg, r, gy, x0, rmin, r0, rn, lane);
         }
     }
     __syncthreads();
