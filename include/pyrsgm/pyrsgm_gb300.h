@@ -40,7 +40,7 @@ size_t pyrsgm_gb300_workspace_bytes(int width, int height, int numDisparities);
  * results and return codes as pyrsgm_compute_level; the scratch is one
  * static 32 MiB device array, so a level must fit in it
  * (pyrsgm_gb300_workspace_bytes(width, height, numDisparities) <= 32 MiB,
- * e.g. 640x480 at 16 labels) or the call returns -1.  The first call on a
+ * e.g. 480x360 at 16 labels) or the call returns -1.  The first call on a
  * device looks up the array's device address (make it before any stream
  * capture).  All calls share the array: calls whose GPU work overlaps race
  * and must be serialised by the caller. */

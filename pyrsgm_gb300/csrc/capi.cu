@@ -52,8 +52,8 @@ static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 size_t Workspace::bytes_for(int w, int h, int D)
 {
     const size_t px = (size_t)w * h;
-    return align256(px * 16) * 2 + align256(px * 2) + align256(px * D * 2) * 2 + align256(px * 2) +
-           align256(px * 4) * 2 + align256(256 * 4);
+    return align256(px * 16) * 2 + align256(px * 2) + align256(px * D * 2) * (uses_packed(D) ? 4 : 2) +
+           align256(px * 2) + align256(px * 4) * 2 + align256(256 * 4);
 }
 
 int Workspace::ensure(int w, int h, int D)
@@ -80,6 +80,11 @@ void Workspace::carve(unsigned char* p, int w, int h, int D)
     base = reinterpret_cast<int16_t*>(p); p += align256(px * 2);
     C = reinterpret_cast<int16_t*>(p); p += align256(px * D * 2);
     V = reinterpret_cast<int16_t*>(p); p += align256(px * D * 2);
+    Vl = Vr = nullptr;
+    if (uses_packed(D)) {
+        Vl = reinterpret_cast<int16_t*>(p); p += align256(px * D * 2);
+        Vr = reinterpret_cast<int16_t*>(p); p += align256(px * D * 2);
+    }
     disp_raw = reinterpret_cast<int16_t*>(p); p += align256(px * 2);
     conf_raw = reinterpret_cast<float*>(p); p += align256(px * 4);
     keys = reinterpret_cast<unsigned*>(p); p += align256(px * 4);
@@ -112,6 +117,8 @@ void fill_workspace_ptrs(LevelDesc& d, const Workspace& ws)
     d.base = ws.base;
     d.C = ws.C;
     d.V = ws.V;
+    d.Vl = ws.Vl;
+    d.Vr = ws.Vr;
     d.disp_raw = ws.disp_raw;
     d.conf_raw = ws.conf_raw;
     d.keys = ws.keys;

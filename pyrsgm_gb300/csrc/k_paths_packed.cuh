@@ -30,19 +30,16 @@
 // the NW + 2 words of its shifted window (word w of chain c at w * CPW + c, so
 // a one-thread chain touches only its own bank).  Chains of T > 1 threads
 // double-buffer the window and exchange it with one __syncwarp per step;
-// their minima and argmins reduce by __shfl_xor_sync.
+// their minima reduce by __shfl_xor_sync.
 //
 // Loads: per thread a ring of kStages steps in shared memory filled with
-// cp.async (costs, partial sums, label base, image byte), so the loads of
-// a step are issued kStages - 1 steps before it without holding registers.
+// cp.async (costs, label base, image byte), so the loads of a step are
+// issued kStages - 1 steps before it without holding registers.
 //
-// Horizontal pass: a warp holds 16/T rows, each with an L->R chain group
-// and an R->L chain group walking towards each other.  The first chain at a
-// pixel leaves its partial sum (with the top->bottom costs) in V; the
-// second reads it back (from the ring, or with a plain load after the
-// per-step __syncwarp when the first wrote it less than kStages + 2 steps
-// earlier), adds its own costs and picks the winner.  The pixel both reach
-// at the same step is finished after the walk.  disp2 candidates go to the
+// Paths: the T->B chains write their costs into V, the L->R and R->L chains
+// of each row into Vl and Vr; the chains never exchange data.  The WTA
+// kernel adds the three (one cap and one sentinel make the clamped sum
+// order-free), picks the winner and writes the disp2 candidates to the
 // per-pixel keys with atomicMin; the LR check reads them in the post kernel.
 #pragma once
 
@@ -109,12 +106,11 @@ struct Grp {
     static constexpr int LENW = PADW + D + 2;   // words a shifted window can touch
     static constexpr int BUFW = LENW * CPW;     // one window buffer of a warp
     static constexpr int NBUF = T == 1 ? 1 : 2;
-    // Ring slot of a thread: costs [0, NW), partial sums [NW, 2NW); strides
-    // chosen so that the 16- or 8-byte lane accesses of a warp hit distinct
-    // banks.  The label-base and image words of a slot sit in a separate
-    // [slot][2][32] array (bank = lane).
-    static constexpr int RSW = NW == 8 ? 20 : (NW == 4 ? 12 : 6);
-    static constexpr int RSW_TB = NW == 8 ? 12 : NW;  // costs only
+    // Ring slot of a thread: its NW cost words, at a stride that puts the
+    // 16- or 8-byte lane accesses of a warp in distinct banks.  The
+    // label-base and image words of a slot sit in a separate [slot][2][32]
+    // array (bank = lane).
+    static constexpr int RSW_TB = NW == 8 ? 12 : NW;
 };
 
 template <int NW>
@@ -319,8 +315,7 @@ template <int NW, int T>
 constexpr size_t row_smem()
 {
     using G = Grp<NW, T>;
-    return 256 * 4 +
-           (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStages * 32 * (G::RSW + 2) + (G::CPW / 2) * (G::D / 2));
+    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStages * 32 * (G::RSW_TB + 2));
 }
 template <int NW, int T>
 constexpr size_t tb_smem()
@@ -420,22 +415,23 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
 }
 
 // ---------------------------------------------------------------------------
-// Horizontal pass: a warp holds 16/T rows; per row an L->R group and an
-// R->L group of T threads.
+// Horizontal paths: a warp holds 16/T rows, each with an L->R chain group
+// and an R->L chain group of T threads.  Each chain walks its whole range
+// and stores its path costs (L->R into Vl, R->L into Vr); the chains of a
+// row never exchange data, and the WTA kernel adds the paths.
 // ---------------------------------------------------------------------------
 template <int NW, int T, bool PYR, int NJ>
 __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant__ Jobs<NJ> jobs)
 {
     using namespace pk;
     using G = Grp<NW, T>;
-    constexpr int D = G::D, RPW = G::CPW / 2, S = kStages, RS = G::RSW;
+    constexpr int D = G::D, RPW = G::CPW / 2, S = kStages, RS = G::RSW_TB;
     const LevelDesc& J = jobs.d[blockIdx.y];
     extern __shared__ __align__(16) uint32_t smem[];
     int* lut = reinterpret_cast<int*>(smem);
     uint32_t* cbuf = smem + 256;
     uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
     uint32_t* bibuf = rbuf + kWarps * S * 32 * RS;
-    uint32_t* mbuf = bibuf + kWarps * S * 64;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
     for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
     __syncthreads();
@@ -450,7 +446,6 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
     uint32_t* ring = rbuf + (warp * S * 32 + lane) * RS;
     uint32_t* bi = bibuf + warp * S * 64 + lane;   // [slot][base, image][lane]
-    uint32_t* mid = mbuf + (warp * RPW + r) * (D / 2);
 
     // path extents (single-scale: kernel_AggregateLR/RL ranges)
     int lr_x0 = 0, lr_n, rl_n;
@@ -463,29 +458,12 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
         lr_n = J.paths >= 2 ? imax(0, maxX1 - minX1) : 0;
         rl_n = imax(0, W - minX1);
     }
-    const bool has_lr = lr_n > 0, has_tb = J.paths >= 3;
     const int n_mine = dir == 0 ? lr_n : rl_n;
     const int Tn = imax(lr_n, rl_n);
-    // Step t of this chain is at x = xs + dx * t.  With M = w - 1 - lr_x0 the
-    // L->R chain reaches x at step x - lr_x0 and the R->L chain at step
-    // w - 1 - x, so both are first for 2t < M and second for 2t > M; at
-    // 2t == M both reach the same pixel (L->R leaves its sum, R->L finishes
-    // after the walk).  R->L steps before t0 are outside the L->R range.
     const int dx = dir == 0 ? 1 : -1;
-    const int xs = dir == 0 ? lr_x0 : W - 1;
-    const int M = W - 1 - lr_x0;
-    const int t0 = (dir == 1 && has_lr) ? W - lr_x0 - lr_n : 0;
-    // 0 nothing, 1 first, 2 second, 3 R->L alone, 4 R->L meets L->R at the same step
-    auto role = [&](int t) -> int {
-        if (t >= n_mine || t < t0) return 0;
-        if (!has_lr) return 3;
-        const int tt = 2 * t;
-        return tt < M ? 1 : (tt == M ? (dir ? 4 : 1) : 2);
-    };
-    // the first chain left its partial less than S + 2 steps before: read it after the step's __syncwarp
-    auto late = [&](int t) { return abs(2 * t - M) <= S + 1; };
+    const int xs = dir == 0 ? lr_x0 : W - 1;   // step t of this chain is at x = xs + dx * t
     const int16_t* const Cg = J.C;
-    int16_t* const Vg = J.V;
+    int16_t* const Og = dir == 0 ? J.Vl : J.Vr;
     const int16_t* const Bg = J.base;
     const uint8_t* const Lg = J.left;
     const bool use_base = PYR && J.refine, adaptive = J.adaptive != 0;
@@ -497,21 +475,9 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     size_t oi = (prow + xs) * D + 2 * NW * k, pi = prow + xs, li = lrow + xs;
     size_t oc = oi, pc = pi, lc = li;
     int ti = 0;
-    // MODE 0: role per step; 1: every chain of the warp is first, not late;
-    // 2: every chain is second, not late (see the loop split below)
-    auto issue_next = [&](int slot, auto mode) {
-        constexpr int MODE = decltype(mode)::value;
-        if (MODE == 1 || ti < n_mine) {
-            uint32_t* d = ring + slot * 32 * RS;
-            cpw<NW>(d, Cg + oi);
-            if (MODE == 1) {
-                if (has_tb) cpw<NW>(d + NW, Vg + oi);
-            } else if (MODE == 2) {
-                cpw<NW>(d + NW, Vg + oi);
-            } else {
-                const int ro = role(ti);
-                if ((ro == 1 && has_tb) || (ro == 2 && !late(ti))) cpw<NW>(d + NW, Vg + oi);
-            }
+    auto issue_next = [&](int slot) {
+        if (ti < n_mine) {
+            cpw<NW>(ring + slot * 32 * RS, Cg + oi);
             if (use_base) cp4(bi + slot * 64, word_of(Bg + pi));
             if (adaptive) cp4(bi + slot * 64 + 32, word_of(Lg + li));
         }
@@ -526,20 +492,15 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
     GChain<NW> s;
     gchain_init(s, minD);
 #pragma unroll
-    for (int j = 0; j < S - 1; ++j) issue_next(j, std::integral_constant<int, 0>{});
+    for (int j = 0; j < S - 1; ++j) issue_next(j);
     int img_prev = 0, slot = 0, islot = S - 1;
-    bool defer = false;
-    int xm = 0;
-    auto step = [&](int t, auto mode) {
-        constexpr int MODE = decltype(mode)::value;
-        issue_next(islot, mode);
+    for (int t = 0; t < Tn; ++t) {
+        issue_next(islot);
         islot = islot + 1 == S ? 0 : islot + 1;
         cp_wait<S - 1>();
-        if (T == 1) __syncwarp();   // orders the other chain's partial sums before the late reads below
         const uint32_t* d = ring + slot * 32 * RS;
         const uint32_t* db = bi + slot * 64;
         slot = slot + 1 == S ? 0 : slot + 1;
-        const int x = xs + dx * t;
         uint32_t cc[NW];
         ldw<NW>(d, cc);
         const int base = use_base ? (int)(int16_t)(db[0] >> ((pc & 1) * 16)) : minD;
@@ -551,75 +512,21 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
         }
         if (PYR && !J.refine) {
             int lo, hi;
-            label_range(J, x, minD, lo, hi);
+            label_range(J, xs + dx * t, minD, lo, hi);
             mask_labels<NW>(cc, lo, hi, k);
         }
-        uint32_t* cw = chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0);
-        gstep<NW, T, PYR>(s, cc, base, p2, p12, cw, k);
-        uint32_t* vp = reinterpret_cast<uint32_t*>(Vg + oc);
-        const int ro = MODE == 0 ? role(t) : MODE;
-        if (ro == 1) {
-            uint32_t part[NW];
-            if (has_tb) {
-                uint32_t vin[NW];
-                ldw<NW>(d + NW, vin);
-#pragma unroll
-                for (int i = 0; i < NW; ++i) part[i] = gcombine<PYR>(s.L[i], vin[i]);
-            } else {
-#pragma unroll
-                for (int i = 0; i < NW; ++i) part[i] = s.L[i];
-            }
-            if (row_ok) stw<NW>(vp, part);
-        } else if (ro == 2) {
-            uint32_t part[NW], tot[NW];
-            if (MODE == 0 && late(t)) ldw<NW>(vp, part);
-            else ldw<NW>(d + NW, part);
-#pragma unroll
-            for (int i = 0; i < NW; ++i) tot[i] = gcombine<PYR>(part[i], s.L[i]);
-            if (row_ok) stw<NW>(vp, tot);
-        } else if (ro == 4) {
-            stw<NW>(mid + NW * k, s.L);
-            defer = true;
-            xm = x;
-        } else if (ro == 3) {
-            if (row_ok) stw<NW>(vp, s.L);
-        }
+        gstep<NW, T, PYR>(s, cc, base, p2, p12, chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0), k);
+        if (t < n_mine && row_ok) stw<NW>(reinterpret_cast<uint32_t*>(Og + oc), s.L);
         oc += dxD;
         pc += dx;
         lc += dx;
-    };
-    // Steps [ta, tb): all chains first and their loads S - 1 steps ahead too;
-    // [tc, td): all chains second, past the late zone; the rest per step.
-    int ta = 0, tb = 0, tc = 0, td = 0;
-    if (has_lr) {
-        ta = W - lr_x0 - lr_n;                                   // R->L reaches the L->R range
-        tb = imax(ta, imin((M - S - 1 + 1) / 2, lr_n) - (S - 1)); // before the late zone, loads included
-        tc = imax(tb, (M + S + 1) / 2 + 1);                       // after the late zone
-        td = imax(tc, imin(lr_n, rl_n));
     }
-    int t = 0;
-    for (; t < ta; ++t) step(t, std::integral_constant<int, 0>{});
-    for (; t < tb; ++t) step(t, std::integral_constant<int, 1>{});
-    for (; t < tc; ++t) step(t, std::integral_constant<int, 0>{});
-    for (; t < td; ++t) step(t, std::integral_constant<int, 2>{});
-    for (; t < Tn; ++t) step(t, std::integral_constant<int, 0>{});
     cp_wait<0>();
-    __syncwarp();
-    if (defer && row_ok) {
-        // the pixel both paths reach at the same step: R->L finishes it
-        uint32_t part[NW], lm[NW], tot[NW];
-        uint32_t* vp = reinterpret_cast<uint32_t*>(Vg + (prow + xm) * D + 2 * NW * k);
-        ldw<NW>(vp, part);
-        ldw<NW>(mid + NW * k, lm);
-#pragma unroll
-        for (int i = 0; i < NW; ++i) tot[i] = gcombine<PYR>(part[i], lm[i]);
-        stw<NW>(vp, tot);
-    }
 }
 
 // ---------------------------------------------------------------------------
 // Winner-take-all of the packed levels, one thread per pixel, from the
-// totals of the three paths in V (kernel_WTA_Subpixel,
+// path costs in V (T->B), Vl and Vr (kernel_WTA_Subpixel,
 // src/sgm_kernels.cu:573-640; pyramid kernel_PyramidWTA,
 // src/sgm_kernels.cu:1290-1370).  Keys (cost << 7 | label) order by cost,
 // then label, so one min tree gives the minimum and its first label.
@@ -637,20 +544,55 @@ __global__ void __launch_bounds__(256) k_wta(const __grid_constant__ Jobs<NJ> jo
     if (x >= J.w || y >= J.h) return;
     const int W = J.w;
     const size_t p = (size_t)y * W + x;
+    const int16_t inv = (int16_t)((J.minD - 1) * 16);
+    bool wta = true;
     if (!PYR) {
+        // the reference defines the aggregated volume on [minX1, maxX1)
+        // (on [minX1, w) with one path) and picks winners on [minX1, maxX1)
+        // except the last column
         const int minX1 = imax(J.minD + D, 0), maxX1 = W + imin(J.minD, 0);
-        if (!(x >= minX1 && x < maxX1 && x != W - 1)) {
-            J.disp_raw[p] = (int16_t)((J.minD - 1) * 16);
+        const int accEnd = J.paths >= 2 ? maxX1 : W;
+        wta = x >= minX1 && x < maxX1 && x != W - 1;
+        if (!(x >= minX1 && x < accEnd)) {
+            J.disp_raw[p] = inv;
             J.conf_raw[p] = 0.0f;
             return;
         }
     }
-    const int16_t* tv = J.V + p * D;
+    // three-path totals (order-free: one cap, SHRT_MAX sentinel)
     uint32_t t[DW];
+    auto load = [&](const int16_t* v, uint32_t (&o)[DW]) {
 #pragma unroll
-    for (int i = 0; i < DW / 4; ++i) {
-        const uint4 q = __ldg(reinterpret_cast<const uint4*>(tv) + i);
-        t[4 * i] = q.x; t[4 * i + 1] = q.y; t[4 * i + 2] = q.z; t[4 * i + 3] = q.w;
+        for (int i = 0; i < DW / 4; ++i) {
+            const uint4 q = __ldg(reinterpret_cast<const uint4*>(v + p * D) + i);
+            o[4 * i] = q.x; o[4 * i + 1] = q.y; o[4 * i + 2] = q.z; o[4 * i + 3] = q.w;
+        }
+    };
+    load(J.Vr, t);
+    if (J.paths >= 2) {
+        uint32_t u[DW];
+        load(J.Vl, u);
+#pragma unroll
+        for (int i = 0; i < DW; ++i) t[i] = gcombine<PYR>(u[i], t[i]);
+    }
+    if (J.paths >= 3) {
+        uint32_t u[DW];
+        load(J.V, u);
+#pragma unroll
+        for (int i = 0; i < DW; ++i) t[i] = gcombine<PYR>(u[i], t[i]);
+    }
+    __shared__ uint32_t tsh[DW * 256];   // word i of thread j at i * 256 + j
+#pragma unroll
+    for (int i = 0; i < DW; ++i) tsh[i * 256 + threadIdx.x] = t[i];
+    if (J.debug_acc) {
+#pragma unroll
+        for (int i = 0; i < DW / 4; ++i)
+            reinterpret_cast<uint4*>(J.V + p * D)[i] = make_uint4(t[4 * i], t[4 * i + 1], t[4 * i + 2], t[4 * i + 3]);
+    }
+    if (!wta) {
+        J.disp_raw[p] = inv;
+        J.conf_raw[p] = 0.0f;
+        return;
     }
     auto key = [&](int d) -> unsigned {
         const uint32_t w = t[d >> 1];
@@ -667,8 +609,11 @@ __global__ void __launch_bounds__(256) k_wta(const __grid_constant__ Jobs<NJ> jo
         a = umin(a, near ? 0xffffffffu : key(d));
     }
     const int alt = (int)(a >> 7);
-    const int c0 = bestD > 0 ? (int)__ldg(tv + bestD - 1) : 0;
-    const int c2 = bestD + 1 < D ? (int)__ldg(tv + bestD + 1) : 0;
+    auto half = [&](int d) -> int {
+        return (int)((tsh[(d >> 1) * 256 + threadIdx.x] >> ((d & 1) * 16)) & 0xffffu);
+    };
+    const int c0 = bestD > 0 ? half(bestD - 1) : 0;
+    const int c2 = bestD + 1 < D ? half(bestD + 1) : 0;
     const int base = (PYR && J.refine) ? (int)J.base[p] : J.minD;
     wta_out<D, PYR>(J, y, x, base, minCost, bestD, alt, c0, minCost, c2);
 }
@@ -708,14 +653,13 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     k_grow<NW, T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(jobs);
     count_launch();
     if (prof_enabled()) {
-        // algorithmic bytes: both horizontal paths read the cost volume, the
-        // top->bottom sums are read once and the totals written once (the
-        // partial sums of the meeting scheme are extra traffic, not counted)
+        // algorithmic bytes: each horizontal path reads the cost volume and
+        // writes its costs once
         double by = 0;
         for (int i = 0; i < jobs.n; ++i) {
             const LevelDesc& d = jobs.d[i];
             const double px = (double)d.w * d.h;
-            by += px * d.D * 2 * (2 + (d.paths >= 3 ? 1 : 0) + 1) + px * 2 * ((d.refine ? 2 : 0) + (d.adaptive ? 1 : 0));
+            by += px * d.D * 2 * (d.paths >= 2 ? 4 : 2) + px * 2 * ((d.refine ? 2 : 0) + (d.adaptive ? 1 : 0));
         }
         prof_end(PK_PATH_ROW, by, st);
     }
@@ -724,7 +668,7 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     prof_begin(st);
     k_wta<G::D, PYR, NJ><<<gw, 256, 0, st>>>(jobs);
     count_launch();
-    prof_end(PK_WTA, jobs_vox(jobs) * 2 + jobs_px(jobs) * (2 + 6 + 4), st);
+    prof_end(PK_WTA, jobs_vox(jobs) * 2 * (jobs.d[0].paths >= 3 ? 3 : jobs.d[0].paths) + jobs_px(jobs) * (2 + 6 + 4), st);
     return cudaGetLastError();
 }
 

@@ -14,8 +14,9 @@
 // Limit.  The scratch is kNoAllocScratchBytes = 32 MiB.  Every GPU on which
 // the library's device code is loaded holds it until the process exits.  A
 // level fits when its workspace size -- pyrsgm_gb300_workspace_bytes(w, h, D),
-// about w*h*(4*D + 24) bytes -- is at most 32 MiB, e.g. 640x480 with 16
-// labels or 320x240 with 64 labels.  Larger levels are rejected with -1 and
+// about w*h*(8*D + 44) bytes for 16/32/64 labels, w*h*(4*D + 44) otherwise --
+// is at most 32 MiB, e.g. 480x360 with 16 labels or 256x192 with 64
+// labels.  Larger levels are rejected with -1 and
 // a message on stderr before any device work.
 //
 // Set-up.  Host code cannot use the array's name as a device address (on the

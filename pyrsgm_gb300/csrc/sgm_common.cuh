@@ -10,9 +10,12 @@
 //   label base        int16 per pixel (refine levels); kNoParent marks pixels
 //                     whose parent was rejected (no valid label)
 //   cost volume C     int16 [y][x][D], d innermost
-//   aggregation V     int16 [y][x][D]: top->bottom path costs, then the
-//                     partial sums of whichever horizontal path reaches a
-//                     pixel first (final totals in debug mode)
+//   aggregation V     int16 [y][x][D]: top->bottom path costs, then (other
+//                     label counts) the partial sums of whichever
+//                     horizontal path reaches a pixel first; final totals in
+//                     debug mode
+//   Vl, Vr            int16 [y][x][D]: L->R and R->L path costs of the
+//                     16/32/64-label levels (summed by the WTA kernel)
 //   disp_raw/conf_raw int16 / float per pixel (pitch = width)
 #pragma once
 
@@ -40,6 +43,8 @@ struct LevelDesc {
     int16_t* base;
     int16_t* C;
     int16_t* V;
+    int16_t* Vl;      // L->R path sums (packed levels)
+    int16_t* Vr;      // R->L path sums (packed levels)
     int16_t* disp_raw;
     float* conf_raw;
     unsigned* keys;   // disp2 candidates: (cost << 16 | 0xFFFF - x) per right-image pixel

@@ -4,6 +4,7 @@
 //   base          int16  [h][w]     refine label base (kNoParent = rejected)
 //   C             int16  [h][w][D]  matching cost
 //   V             int16  [h][w][D]  aggregation volume
+//   Vl, Vr        int16  [h][w][D]  L->R and R->L path sums (16/32/64 labels only)
 //   disp_raw      int16  [h][w]     disparity*16 before the median
 //   conf_raw      float  [h][w]     confidence before the median reset
 //   keys          u32    [h][w]     disp2 candidates (cost << 16 | 0xFFFF - x)
@@ -30,6 +31,8 @@ struct Workspace {
     int16_t* base = nullptr;
     int16_t* C = nullptr;
     int16_t* V = nullptr;
+    int16_t* Vl = nullptr;
+    int16_t* Vr = nullptr;
     int16_t* disp_raw = nullptr;
     float* conf_raw = nullptr;
     unsigned* keys = nullptr;
