@@ -90,30 +90,25 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
     const int tx = threadIdx.x & (kFtX - 1), ty = threadIdx.x / kFtX;
     const int x = x0 + tx, y = y0 + ty;
     if (x >= W || y >= H) return;
-    // pixel (gy, gx), both already clamped to the image
-    auto px = [&](int gy, int gx) -> int { return t[gy - y0 + kFtHalo][gx - x0 + kFtHalo]; };
+    // Tile entry (ty + 2 + dy, tx + 2 + dx) holds pixel (clamp(y + dy),
+    // clamp(x + dx)): the replicate-border neighbours need no clamping here.
     const size_t p = (size_t)y * W + x;
     if (J.cost == COST_CENSUS) {
-        const int c = px(y, x);
+        const int c = t[ty + 2][tx + 2];
         uint32_t cv = 0;
 #pragma unroll
         for (int dy = 0; dy < 5; ++dy) {
-            const int gy = iclamp(y + dy - 2, 0, H - 1);
 #pragma unroll
-            for (int dx = 0; dx < 5; ++dx) {
-                cv <<= 1;
-                cv |= (uint32_t)(px(gy, iclamp(x + dx - 2, 0, W - 1)) < c);
-            }
+            for (int dx = 0; dx < 5; ++dx) cv = (cv << 1) | (uint32_t)(t[ty + dy][tx + dx] < c);
         }
         reinterpret_cast<uint32_t*>(feat)[p] = cv;
     } else {
         const int ftzero = imax(J.pfc, 15) | 1;
-        const int yp = imax(y - 1, 0), yn = imin(y + 1, H - 1);
-        auto grad = [&](int gx) -> int {
-            const int xp = imax(gx - 1, 0), xn = imin(gx + 1, W - 1);
-            int g = (px(y, xn) - px(y, xp)) * 2;
-            g += px(yp, xn) - px(yp, xp);
-            g += px(yn, xn) - px(yn, xp);
+        // gradient at tile column c of row y (its neighbours clamped to the image)
+        auto grad = [&](int c) -> int {
+            int g = (t[ty + 2][c + 1] - t[ty + 2][c - 1]) * 2;
+            g += t[ty + 1][c + 1] - t[ty + 1][c - 1];
+            g += t[ty + 3][c + 1] - t[ty + 3][c - 1];
             return iclamp(g, -ftzero, ftzero) + ftzero;
         };
         // value, lo, hi of one channel as 16-bit fields
@@ -122,11 +117,12 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
             lo = (uint32_t)imin(imin(vl, vr), v);
             hi = (uint32_t)imax(imax(vl, vr), v);
         };
-        const int xm = imax(x - 1, 0), xq = imin(x + 1, W - 1);
-        const int gv = grad(x), iv = px(y, x);
+        // the neighbour columns are clamped first (x - 1 -> 0 at the left border)
+        const int cc = tx + 2, cm = x > 0 ? cc - 1 : cc, cq = x + 1 < W ? cc + 1 : cc;
+        const int gv = grad(cc), iv = t[ty + 2][cc];
         uint32_t glo, ghi, ilo, ihi;
-        interval(gv, grad(xm), grad(xq), glo, ghi);
-        interval(iv, px(y, xm), px(y, xq), ilo, ihi);
+        interval(gv, grad(cm), grad(cq), glo, ghi);
+        interval(iv, t[ty + 2][cm], t[ty + 2][cq], ilo, ihi);
         const uint32_t X = (uint32_t)gv | ((uint32_t)iv << 16), X0 = glo | (ilo << 16), X1 = ghi | (ihi << 16);
         feat[p] = make_uint4(X + kBtBias2, X, X0 + kBtBias2, X1);
     }
