@@ -2,6 +2,8 @@
 // refine-label preparation, the adaptive-P2 table and the matching-cost
 // volume.  Integer arithmetic, clamps and sentinels follow the reference
 // kernels cited at each function (reference file:line).
+#include <type_traits>
+
 #include "profiler.h"
 #include "sgm_common.cuh"
 #include "sgm_launch.h"
@@ -354,27 +356,41 @@ __device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, ui
     __syncwarp();
     const int ri = r0 + lane;
     const int real = rmin + ri;
-    int q[2 * HW + 1];   // q[0 .. 2HW-1]: the last 2HW costs, oldest first
-#pragma unroll
-    for (int i = 0; i < 2 * HW + 1; ++i) q[i] = 0;
-    int s = 0;
     uint16_t* out = hs + (size_t)r * kTiX * kTiRs + ri;
-#pragma unroll 4
-    for (int j = 0; j < SW; ++j) {
-        const int gx = iclamp(x0 - HW + j, 0, W - 1);
-        const int x2 = gx - real;
-        const int e = (x2 >= 0 && x2 < W) ? bt_pixel(sl[j], sr[x2 - xr0]) : 255;
-        s += e;
-        if (j >= 2 * HW && ri < rn) out[(j - 2 * HW) * kTiRs] = (uint16_t)s;
-        if (HW > 0) {
-            s -= q[0];
+    const bool store = ri < rn;
+    // every window column inside the image and every right pixel too: no clamps, no range checks
+    const bool interior = x0 - HW >= 0 && x0 + kTiX - 1 + HW < W && xr0 >= 0 && xr0 + SW + 30 < W;
+    auto walk = [&](auto inner) {
+        constexpr bool IN = decltype(inner)::value;
+        const uint4* srl = sr + (31 - lane);   // right pixel of column j: srl[j] (interior)
+        int q[2 * HW + 1];                     // q[0 .. 2HW-1]: the last 2HW costs, oldest first
 #pragma unroll
-            for (int i = 0; i + 1 < 2 * HW; ++i) q[i] = q[i + 1];
-            q[2 * HW - 1 < 0 ? 0 : 2 * HW - 1] = e;
-        } else {
-            s = 0;
+        for (int i = 0; i < 2 * HW + 1; ++i) q[i] = 0;
+        int s = 0;
+#pragma unroll
+        for (int j = 0; j < SW; ++j) {
+            int e;
+            if (IN) {
+                e = bt_pixel(sl[j], srl[j]);
+            } else {
+                const int gx = iclamp(x0 - HW + j, 0, W - 1);
+                const int x2 = gx - real;
+                e = (x2 >= 0 && x2 < W) ? bt_pixel(sl[j], sr[x2 - xr0]) : 255;
+            }
+            s += e;
+            if (j >= 2 * HW && store) out[(j - 2 * HW) * kTiRs] = (uint16_t)s;
+            if (HW > 0) {
+                s -= q[0];
+#pragma unroll
+                for (int i = 0; i + 1 < 2 * HW; ++i) q[i] = q[i + 1];
+                q[2 * HW - 1 < 0 ? 0 : 2 * HW - 1] = e;
+            } else {
+                s = 0;
+            }
         }
-    }
+    };
+    if (interior) walk(std::true_type{});
+    else walk(std::false_type{});
     __syncwarp();   // the staging buffer is refilled by the warp's next unit
 }
 
