@@ -57,7 +57,10 @@ namespace pk {
 
 constexpr uint32_t kMax2 = 0x7fff7fffu;
 constexpr uint32_t kOne2 = 0x00010001u;
-constexpr int kWarps = 4;        // warps per block
+// Warps per block: 4 for the one-thread-per-16-labels shape (throughput on
+// many rows), 2 for the spread shapes (more, smaller blocks for few rows).
+template <int NW>
+__host__ __device__ constexpr int warps_of() { return NW == 8 ? 4 : 2; }
 constexpr int kStages = 6;       // look-ahead of the horizontal pass (steps)
 constexpr int kStagesTb = 8;     // look-ahead of the top->bottom pass
 
@@ -315,13 +318,13 @@ template <int NW, int T>
 constexpr size_t row_smem()
 {
     using G = Grp<NW, T>;
-    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStages * 32 * (G::RSW_TB + 2));
+    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + kStages * 32 * (G::RSW_TB + 2));
 }
 template <int NW, int T>
 constexpr size_t tb_smem()
 {
     using G = Grp<NW, T>;
-    return 256 * 4 + (size_t)kWarps * 4 * (G::NBUF * G::BUFW + kStagesTb * 32 * (G::RSW_TB + 2));
+    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + kStagesTb * 32 * (G::RSW_TB + 2));
 }
 
 }  // namespace pk
@@ -330,11 +333,11 @@ constexpr size_t tb_smem()
 // Top -> bottom: a warp holds 32/T adjacent columns, T threads each.
 // ---------------------------------------------------------------------------
 template <int NW, int T, bool PYR, int NJ>
-__global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__ Jobs<NJ> jobs)
+__global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_gtb(const __grid_constant__ Jobs<NJ> jobs)
 {
     using namespace pk;
     using G = Grp<NW, T>;
-    constexpr int D = G::D, S = kStagesTb, RS = G::RSW_TB;
+    constexpr int D = G::D, S = kStagesTb, RS = G::RSW_TB, kWarps = warps_of<NW>();
     const LevelDesc& J = jobs.d[blockIdx.y];
     extern __shared__ __align__(16) uint32_t smem[];
     int* lut = reinterpret_cast<int*>(smem);
@@ -388,6 +391,7 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
 #pragma unroll
     for (int j = 0; j < S - 1; ++j) issue_next(j);
     int img_prev = 0, slot = 0, islot = S - 1;
+#pragma unroll 2
     for (int y = 0; y < H; ++y) {
         issue_next(islot);
         islot = islot + 1 == S ? 0 : islot + 1;
@@ -421,11 +425,11 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_gtb(const __grid_constant__
 // row never exchange data, and the WTA kernel adds the paths.
 // ---------------------------------------------------------------------------
 template <int NW, int T, bool PYR, int NJ>
-__global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant__ Jobs<NJ> jobs)
+__global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_constant__ Jobs<NJ> jobs)
 {
     using namespace pk;
     using G = Grp<NW, T>;
-    constexpr int D = G::D, RPW = G::CPW / 2, S = kStages, RS = G::RSW_TB;
+    constexpr int D = G::D, RPW = G::CPW / 2, S = kStages, RS = G::RSW_TB, kWarps = warps_of<NW>();
     const LevelDesc& J = jobs.d[blockIdx.y];
     extern __shared__ __align__(16) uint32_t smem[];
     int* lut = reinterpret_cast<int*>(smem);
@@ -494,6 +498,7 @@ __global__ void __launch_bounds__(pk::kWarps * 32) k_grow(const __grid_constant_
 #pragma unroll
     for (int j = 0; j < S - 1; ++j) issue_next(j);
     int img_prev = 0, slot = 0, islot = S - 1;
+#pragma unroll 2
     for (int t = 0; t < Tn; ++t) {
         issue_next(islot);
         islot = islot + 1 == S ? 0 : islot + 1;
@@ -635,10 +640,11 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         if ((err = cudaFuncSetAttribute(k_gtb<NW, T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem)) != cudaSuccess)
             return err;
-        const int cols = pk::kWarps * G::CPW;
+        constexpr int kWarps = pk::warps_of<NW>();
+        const int cols = kWarps * G::CPW;
         dim3 g((e.max_w + cols - 1) / cols, n);
         prof_begin(st);
-        k_gtb<NW, T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(tbj);
+        k_gtb<NW, T, PYR, NJ><<<g, kWarps * 32, smem, st>>>(tbj);
         count_launch();
         prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * ((tbj.d[0].refine ? 2 : 0) + (tbj.d[0].adaptive ? 1 : 0)), st);
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
@@ -647,10 +653,11 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     if ((err = cudaFuncSetAttribute(k_grow<NW, T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
         cudaSuccess)
         return err;
-    const int rows = pk::kWarps * G::CPW / 2;
+    constexpr int kWarps = pk::warps_of<NW>();
+    const int rows = kWarps * G::CPW / 2;
     dim3 g((e.max_h + rows - 1) / rows, jobs.n);
     prof_begin(st);
-    k_grow<NW, T, PYR, NJ><<<g, pk::kWarps * 32, smem, st>>>(jobs);
+    k_grow<NW, T, PYR, NJ><<<g, kWarps * 32, smem, st>>>(jobs);
     count_launch();
     if (prof_enabled()) {
         // algorithmic bytes: each horizontal path reads the cost volume and
