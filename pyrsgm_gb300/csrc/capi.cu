@@ -13,7 +13,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <new>
+#include <utility>
 
 #include "pyrsgm/pyrsgm_c.h"
 #include "pyrsgm/pyrsgm_gb300.h"
@@ -45,6 +47,28 @@ int sm_count()
         slot.store(n, std::memory_order_relaxed);
     }
     return n;
+}
+
+ForkStreams& fork_streams(cudaStream_t st)
+{
+    // one auxiliary stream per (device, main stream) of this thread, so that
+    // work forked from different main streams (server lanes) stays
+    // independent; past 64 main streams they share one
+    static thread_local std::map<std::pair<int, cudaStream_t>, ForkStreams> per;
+    static thread_local ForkStreams none;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+    auto key = std::make_pair(dev, per.size() < 64 ? st : nullptr);
+    auto it = per.find(key);
+    if (it != per.end()) return it->second;
+    ForkStreams f;
+    if (cudaStreamCreateWithFlags(&f.aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return none;
+    }
+    return per.emplace(key, f).first->second;
 }
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }

@@ -630,6 +630,19 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     cudaError_t err;
     bool any_tb = false;
     for (int i = 0; i < jobs.n; ++i) any_tb = any_tb || jobs.d[i].paths >= 3;
+    // T->B and the horizontal paths only share the cost volume.  In the
+    // spread shapes (launches with few rows, which leave most SMs idle) T->B
+    // runs on a second stream beside the row pass, joined before the WTA;
+    // launches that fill the GPU run them one after the other (side by side
+    // they only contend).
+    ForkStreams& fk = fork_streams(st);
+    const bool fork = NW != 8 && any_tb && fk.aux != nullptr;
+    cudaStream_t tbst = st;
+    if (fork) {
+        if ((err = cudaEventRecord(fk.fork, st)) != cudaSuccess) return err;
+        if ((err = cudaStreamWaitEvent(fk.aux, fk.fork, 0)) != cudaSuccess) return err;
+        tbst = fk.aux;
+    }
     if (any_tb) {
         Jobs<NJ> tbj = jobs;
         int n = 0;
@@ -643,10 +656,10 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         constexpr int kWarps = pk::warps_of<NW>();
         const int cols = kWarps * G::CPW;
         dim3 g((e.max_w + cols - 1) / cols, n);
-        prof_begin(st);
-        k_gtb<NW, T, PYR, NJ><<<g, kWarps * 32, smem, st>>>(tbj);
+        prof_begin(tbst);
+        k_gtb<NW, T, PYR, NJ><<<g, kWarps * 32, smem, tbst>>>(tbj);
         count_launch();
-        prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * ((tbj.d[0].refine ? 2 : 0) + (tbj.d[0].adaptive ? 1 : 0)), st);
+        prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * ((tbj.d[0].refine ? 2 : 0) + (tbj.d[0].adaptive ? 1 : 0)), tbst);
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
     }
     constexpr size_t smem = pk::row_smem<NW, T>();
@@ -671,6 +684,10 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         prof_end(PK_PATH_ROW, by, st);
     }
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if (fork) {
+        if ((err = cudaEventRecord(fk.join, fk.aux)) != cudaSuccess) return err;
+        if ((err = cudaStreamWaitEvent(st, fk.join, 0)) != cudaSuccess) return err;
+    }
     dim3 gw((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
     prof_begin(st);
     k_wta<G::D, PYR, NJ><<<gw, 256, 0, st>>>(jobs);

@@ -86,6 +86,17 @@ inline int path_variant(int D)
 
 // Multiprocessor count of the current device (cached per device).
 int sm_count();
+
+// A second stream and two events paired with the main stream `st` (per
+// calling thread and device), for launching independent kernels side by
+// side (fork: record `fork` on st, `aux` waits; join: record `join` on
+// `aux`, st waits).  Under stream capture this becomes two graph branches.
+// Null `aux` when they could not be created: run sequentially.
+struct ForkStreams {
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+ForkStreams& fork_streams(cudaStream_t st);
 // 0 (choose per launch), 8, or 2/4: the packed kernels' words per thread.
 int packed_words_override();
 
