@@ -53,9 +53,9 @@ def params_for(cost: int) -> dict:
 
 
 # DRAM bytes per algorithmic byte of k_grow, from one ncu capture of its
-# level-0 launch for four 1080p pairs (dram read + write 1.460 GB against
-# 1.112 GB algorithmic); the partial sums of the meeting scheme are the extra.
-K_GROW_TRAFFIC_PER_ALG_BYTE = 1.314
+# level-0 launch for four 1080p pairs (dram read + write 1.027 GB against
+# 1.112 GB algorithmic; part of the second read of the cost volume hits L2).
+K_GROW_TRAFFIC_PER_ALG_BYTE = 0.924
 
 
 def peaks() -> dict:
@@ -647,7 +647,7 @@ def run(args) -> dict | None:
         prof = headline["prof"]
         row = prof.get("path_row", {})
         achieved = (row["bytes"] / (row["ms"] / 1e3) / 1e9) if row.get("ms") else None
-        out["roofline"] = {"kernel": "k_grow (L->R + R->L path sums, three-path totals)", "bound": "hbm",
+        out["roofline"] = {"kernel": "k_grow (L->R and R->L path costs of the 16/32-label levels)", "bound": "hbm",
                            "achieved": round(achieved, 2) if achieved else None, "peak": pk["hbm_gbs"],
                            "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4) if achieved else None,
                            "peak_source": pk["source"],
