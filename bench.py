@@ -506,10 +506,18 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
         for o in s_outs:
             for a in o.values():
                 srv.register(a)
-    for k in range(min(4, n)):  # warm the pools
-        l, r, c = pairs_pool[picks[k]]
-        rid, _ = srv.submit(l, r, params_of(c), outputs=outs[(l.shape[1], l.shape[0])][k])
-        srv.wait(rid)
+    # warm the lanes' plan pools: every pool pair in bursts of max_batch, so
+    # that plans for repeated shapes within a batch exist on every lane
+    for rep in range(2 * streams):
+        ids = []
+        for k, (l, r, c) in enumerate(pairs_pool):
+            ids.append(srv.submit(l, r, params_of(c), outputs=outs[(l.shape[1], l.shape[0])][k % nout])[0])
+            if len(ids) == max_batch:
+                for rid in ids:
+                    srv.wait(rid)
+                ids = []
+        for rid in ids:
+            srv.wait(rid)
     srv.reset_stats()
     refused = 0
     t0 = time.perf_counter()
@@ -723,7 +731,8 @@ def serve_sweep(args) -> None:
         cfg.append(pg.Params(num_disparities=D, pyramid_levels=L, cost_mode=c, p1=8 if c else 300,
                              p2=32 if c else 2400))
     for rate in args.rates:
-        res = serve_compare(pool, lambda k: cfg[k], rate, args.serve_requests, seed=int(rate))
+        res = serve_compare(pool, lambda k: cfg[k], rate, args.serve_requests, seed=int(rate),
+                            max_batch=args.serve_batch, streams=args.serve_streams)
         print(json.dumps({"metric": "mixed-stream serving", **res}), flush=True)
 
 
@@ -741,6 +750,8 @@ def main():
                     help="requests of the serving comparison (0 skips it)")
     ap.add_argument("--rates", type=float, nargs="*", default=[500, 1000, 2000, 5000, 10000, 20000])
     ap.add_argument("--pool", type=int, default=24, help="distinct pairs of the serving sweep")
+    ap.add_argument("--serve-batch", type=int, default=16, help="server: largest batch")
+    ap.add_argument("--serve-streams", type=int, default=2, help="server: stream lanes")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
     if args.warmup < 3:
