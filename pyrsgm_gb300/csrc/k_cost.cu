@@ -403,24 +403,51 @@ __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ J
     const int W = J.w, H = J.h, D = J.D, h = J.bs / 2;
     extern __shared__ __align__(16) uint16_t hs[];   // [kTiY + 2h][kTiX][kTiRs], then per warp kTiStage uint4
     uint4* stg = reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(hs) + kTiHs) + (threadIdx.x >> 5) * kTiStage;
-    __shared__ int wred[2][kTiY];
+    __shared__ int wred[4][kTiY];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int x = x0 + lane, y = y0 + warp;
     const bool inside = x < W && y < H;
     const int b = inside ? (int)J.base[(size_t)y * W + x] : (int)kNoParent;
     const bool has = inside && b != kNoParent;
-    const int bmin = __reduce_min_sync(0xffffffffu, has ? b : INT_MAX);
-    const int bmax = __reduce_max_sync(0xffffffffu, has ? b : INT_MIN);
-    if (lane == 0) { wred[0][warp] = bmin; wred[1][warp] = bmax; }
-    __syncthreads();
-    int rmin = INT_MAX, rmax = INT_MIN;
+    auto block_minmax = [&](bool in, int v, int& mn, int& mx) {
+        const int a = __reduce_min_sync(0xffffffffu, in ? v : INT_MAX);
+        const int z = __reduce_max_sync(0xffffffffu, in ? v : INT_MIN);
+        __syncthreads();   // wred reused
+        if (lane == 0) { wred[0][warp] = a; wred[1][warp] = z; }
+        __syncthreads();
+        mn = INT_MAX;
+        mx = INT_MIN;
 #pragma unroll
-    for (int i = 0; i < kTiY; ++i) { rmin = imin(rmin, wred[0][i]); rmax = imax(rmax, wred[1][i]); }
-    const bool any = rmax != INT_MIN;
-    rmax += D - 1;
-    const bool tiled = any && rmax - rmin + 1 <= kTiRn && h <= kTiMaxHalf;
-    if (tiled) {
-        const int rn = rmax - rmin + 1;
+        for (int i = 0; i < kTiY; ++i) { mn = imin(mn, wred[0][i]); mx = imax(mx, wred[1][i]); }
+    };
+    // Real disparities the tile needs: [min base, max base + D - 1].  When
+    // they span more than kTiRn (a depth edge through the tile), the bases
+    // are split at the midpoint of their range into two clusters, each
+    // handled by its own pass when it fits.
+    int bmin, bmax;
+    block_minmax(has, b, bmin, bmax);
+    int ncl = 0, cut = INT_MAX;
+    int cmin[2] = {bmin, 0}, cmax[2] = {bmax, 0};
+    if (bmax != INT_MIN && h <= kTiMaxHalf) {
+        if (bmax + D - bmin <= kTiRn) {
+            ncl = 1;
+        } else {
+            cut = bmin + ((bmax - bmin) >> 1);
+            int a0, a1, b0, b1;
+            block_minmax(has && b <= cut, b, a0, a1);
+            block_minmax(has && b > cut, b, b0, b1);
+            if (a1 + D - a0 <= kTiRn && b1 + D - b0 <= kTiRn) {
+                ncl = 2;
+                cmin[0] = a0; cmax[0] = a1; cmin[1] = b0; cmax[1] = b1;
+            }
+        }
+    }
+    int lo, hi;
+    label_range(J, x, b, lo, hi);
+    int16_t* out = J.C + ((size_t)(inside ? y : 0) * W + (inside ? x : 0)) * D;
+    const bool vec = (D & 7) == 0;
+    for (int c = 0; c < ncl; ++c) {
+        const int rmin = cmin[c], rn = cmax[c] + D - cmin[c];
         const int nch = (rn + 31) >> 5;   // 32 real disparities per warp pass
         for (int u = warp; u < (kTiY + 2 * h) * nch; u += kTiY) {
             const int r = u / nch, r0 = (u - r * nch) * 32;
@@ -429,42 +456,38 @@ __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ J
             else if (h == 1) bt_row_sums<1>(J, hs, stg, r, gy, x0, rmin, r0, rn, lane);
             else bt_row_sums<0>(J, hs, stg, r, gy, x0, rmin, r0, rn, lane);
         }
-    }
-    __syncthreads();
-    if (!inside) return;
-    int lo, hi;
-    label_range(J, x, b, lo, hi);
-    int16_t* out = J.C + ((size_t)y * W + x) * D;
-    const bool vec = (D & 7) == 0;
-    if (tiled && b != kNoParent) {
-        // packed pair sums of 2h+1 rows from offset ri0 = b - rmin (halves), 8 labels per chunk
-        const int ri0 = b - rmin;
-        const uint32_t sh = (uint32_t)(ri0 & 1) * 16;
-        for (int d0 = 0; d0 < D; d0 += 8) {
-            uint32_t acc[5] = {0u, 0u, 0u, 0u, 0u};
-            for (int k = 0; k <= 2 * h; ++k) {
-                const uint32_t* row =
-                    reinterpret_cast<const uint32_t*>(hs + ((warp + k) * kTiX + lane) * kTiRs) + ((ri0 + d0) >> 1);
+        __syncthreads();
+        if (has && (ncl == 1 || (c == 0) == (b <= cut))) {
+            // packed pair sums of 2h+1 rows from offset ri0 = b - rmin (halves), 8 labels per chunk
+            const int ri0 = b - rmin;
+            const uint32_t sh = (uint32_t)(ri0 & 1) * 16;
+            for (int d0 = 0; d0 < D; d0 += 8) {
+                uint32_t acc[5] = {0u, 0u, 0u, 0u, 0u};
+                for (int k = 0; k <= 2 * h; ++k) {
+                    const uint32_t* row =
+                        reinterpret_cast<const uint32_t*>(hs + ((warp + k) * kTiX + lane) * kTiRs) + ((ri0 + d0) >> 1);
 #pragma unroll
-                for (int j = 0; j < 5; ++j) acc[j] += row[j];
-            }
-            uint32_t w[4];
+                    for (int j = 0; j < 5; ++j) acc[j] += row[j];
+                }
+                uint32_t w[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                w[i] = __funnelshift_r(acc[i], acc[i + 1], sh);
-                const int d = d0 + 2 * i;
-                if (d < lo || d > hi) w[i] = (w[i] & 0xffff0000u) | (uint32_t)kMax;
-                if (d + 1 < lo || d + 1 > hi) w[i] = (w[i] & 0xffffu) | ((uint32_t)kMax << 16);
-            }
-            if (vec) {
-                reinterpret_cast<uint4*>(out + d0)[0] = make_uint4(w[0], w[1], w[2], w[3]);
-            } else {
-                for (int i = 0; i < 8 && d0 + i < D; ++i)
-                    out[d0 + i] = (int16_t)((w[i >> 1] >> ((i & 1) * 16)) & 0xffffu);
+                for (int i = 0; i < 4; ++i) {
+                    w[i] = __funnelshift_r(acc[i], acc[i + 1], sh);
+                    const int d = d0 + 2 * i;
+                    if (d < lo || d > hi) w[i] = (w[i] & 0xffff0000u) | (uint32_t)kMax;
+                    if (d + 1 < lo || d + 1 > hi) w[i] = (w[i] & 0xffffu) | ((uint32_t)kMax << 16);
+                }
+                if (vec) {
+                    reinterpret_cast<uint4*>(out + d0)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                } else {
+                    for (int i = 0; i < 8 && d0 + i < D; ++i)
+                        out[d0 + i] = (int16_t)((w[i >> 1] >> ((i & 1) * 16)) & 0xffffu);
+                }
             }
         }
-        return;
+        __syncthreads();   // the next cluster's row sums overwrite hs
     }
+    if (!inside || (ncl > 0 && has)) return;
     // direct window per pixel
     for (int d0 = 0; d0 < D; d0 += 8) {
         int sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
