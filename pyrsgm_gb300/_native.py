@@ -36,6 +36,15 @@ class Pair(C.Structure):
                 ("d_conf", _vp), ("conf_pitch", _sz), ("width", _i), ("height", _i), ("params", Params)]
 
 
+class Metrics(C.Structure):
+    """pyrsgm_gb300_metrics: disparity metrics against ground truth."""
+    _fields_ = [("evaluated", _i), ("valid", _i)] + [(n, C.c_double) for n in (
+        "avg_err", "rms_err", "bad05", "bad1", "bad2", "bad4", "density", "invalid", "bad1_all", "bad2_all")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class Request(C.Structure):
     """pyrsgm_gb300_request: one served pair (host buffers, pitch = width)."""
     _fields_ = [("h_left", _vp), ("h_right", _vp), ("h_disp16", _vp), ("h_disp32", _vp), ("h_conf", _vp),
@@ -93,6 +102,12 @@ _SIGS = {
     "pyrsgm_gb300_version": (C.c_char_p, []),
     "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
     "pyrsgm_gb300_set_packed_words": (_i, [_i]),
+    "pyrsgm_gb300_read_pfm": (_i, [C.c_char_p, _vp, _sz, C.POINTER(_i), C.POINTER(_i), C.c_char_p, _sz]),
+    "pyrsgm_gb300_write_pfm": (_i, [C.c_char_p, _vp, _sz, _i, _i, C.c_char_p, _sz]),
+    "pyrsgm_gb300_read_pgm": (_i, [C.c_char_p, _vp, _sz, C.POINTER(_i), C.POINTER(_i), C.c_char_p, _sz]),
+    "pyrsgm_gb300_write_pgm": (_i, [C.c_char_p, _vp, _sz, _i, _i, C.c_char_p, _sz]),
+    "pyrsgm_gb300_read_ndisp": (_i, [C.c_char_p]),
+    "pyrsgm_gb300_evaluate": (_i, [_vp, _sz, _vp, _sz, _vp, _sz, _i, _i, _f, C.POINTER(Metrics)]),
     "pyrsgm_gb300_profile": (_i, [_i]),
     "pyrsgm_gb300_profile_read": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
 }

@@ -67,15 +67,33 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, hdr_mtime, verbose), srcs))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
+        tmp = LIB + ".tmp"
+        cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+    build_cli(hdr_mtime)
+    return LIB
+
+
+CLI_SRC = os.path.join(PKG, "cli", "stereo_pair.cpp")
+CLI = os.path.join(PKG, "pyrsgm_stereo_pair")
+
+
+def build_cli(hdr_mtime: float) -> str:
+    """The headless stereo CLI, linked against the library (rpath to it)."""
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(CLI_SRC), os.path.getmtime(LIB),
+                                                             hdr_mtime):
+        return CLI
+    cmd = [nvcc(), "-O2", "-std=c++17", "-x", "cu", CLI_SRC, "-o", CLI + ".tmp", "-I" + os.path.join(ROOT, "include"),
+           "-L" + PKG, "-lpyrsgm_gb300", "-Xlinker", "-rpath=" + PKG] + ARCH
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+        raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 if __name__ == "__main__":
