@@ -704,8 +704,22 @@ def single_pair_latency(dev, stream, runs: int = 20) -> dict:
         if k >= 3:
             ms.append(a.elapsed_time(b))
     m.close()
+    # the opt-in speckle filter on that disparity map (regions <= 100 px, 1 px steps)
+    src = d16.clone()
+    sp = []
+    for k in range(3 + runs):
+        with torch.cuda.stream(stream):
+            d16.copy_(src)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            pg.filter_speckles(d16, pg.invalid_disparity16(p), 100, 16, stream)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if k >= 3:
+            sp.append(a.elapsed_time(b))
     return {"p50_ms": round(_pct(ms, 0.5), 4), "p99_ms": round(_pct(ms, 0.99), 4), "runs": runs,
-            "levels": [(li.width, li.height, li.num_labels) for li in pg.level_geometry(W, H, p)]}
+            "levels": [(li.width, li.height, li.num_labels) for li in pg.level_geometry(W, H, p)],
+            "speckle_filter_p50_ms": round(_pct(sp, 0.5), 4)}
 
 
 MIX_SIZES = [(640, 480), (960, 540), (1280, 720), (1920, 1080)]

@@ -183,6 +183,18 @@ const char* pyrsgm_gb300_version(void);
 /* Kernel launches issued by this library since the process started. */
 unsigned long long pyrsgm_gb300_launch_count(void);
 
+/* Opt-in speckle filter on an int16 disparity map (device pointer, pitch in
+ * bytes), enqueued on `stream`: 4-neighbours belong to one region when
+ * neither equals new_val and their values differ by at most max_diff (in the
+ * map's units, e.g. 16 per pixel for disparity x16); regions of at most
+ * max_speckle_size pixels are set to new_val -- the semantics of OpenCV's
+ * cv::filterSpeckles, which the reference's benchmark leaves off.  Not part
+ * of compute(); max_speckle_size <= 0 does nothing.  Scratch of 8 bytes per
+ * pixel comes from the stream-ordered allocator.  0, or -1 on bad arguments
+ * or a failed allocation/launch. */
+int pyrsgm_gb300_filter_speckles(short* d_disp, size_t pitch_bytes, int width, int height, short new_val,
+                                 int max_speckle_size, int max_diff, cudaStream_t stream);
+
 /* Shape of the 16/32/64-label aggregation kernels: 0 chooses per launch
  * (one thread per 16 labels when the launch has rows enough to fill the
  * GPU, else a chain spread over more threads), 8 forces the former, 2 or 4

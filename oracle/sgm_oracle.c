@@ -1204,3 +1204,53 @@ int orc_matcher_compute(int w, int h, const orc_params* in,
     free(scratch_conf);
     return ret;
 }
+
+/* ---------------------------------------------------------------------------
+ * Speckle filter (no counterpart in the reference library): sequential
+ * 4-connected flood fill from every unlabelled valid pixel, an explicit
+ * stack, then every region of at most max_size pixels set to new_val.
+ * ------------------------------------------------------------------------- */
+int orc_filter_speckles(int16_t* img, size_t step, int width, int height, int16_t new_val, int max_size,
+                        int max_diff)
+{
+    if (!img || width <= 0 || height <= 0 || max_diff < 0) return -1;
+    if (max_size <= 0) return 0;
+    const size_t n = (size_t)width * height;
+    int* lab = (int*)malloc(n * sizeof(int));
+    int* stack = (int*)malloc(n * sizeof(int));
+    int* region = (int*)malloc(n * sizeof(int));
+    if (!lab || !stack || !region) { free(lab); free(stack); free(region); return -1; }
+    for (size_t i = 0; i < n; ++i) lab[i] = -1;
+#define PX(x, y) (*(int16_t*)((uint8_t*)img + (size_t)(y) * step + (size_t)(x) * 2))
+    for (int y0 = 0; y0 < height; ++y0) {
+        for (int x0 = 0; x0 < width; ++x0) {
+            const int s = y0 * width + x0;
+            if (lab[s] >= 0 || PX(x0, y0) == new_val) continue;
+            int top = 0, cnt = 0;
+            stack[top++] = s;
+            lab[s] = s;
+            while (top > 0) {
+                const int p = stack[--top];
+                region[cnt++] = p;
+                const int x = p % width, y = p / width, v = PX(x, y);
+                const int nx[4] = {x - 1, x + 1, x, x};
+                const int ny[4] = {y, y, y - 1, y + 1};
+                for (int k = 0; k < 4; ++k) {
+                    if (nx[k] < 0 || nx[k] >= width || ny[k] < 0 || ny[k] >= height) continue;
+                    const int q = ny[k] * width + nx[k];
+                    const int u = PX(nx[k], ny[k]);
+                    if (lab[q] >= 0 || u == new_val || abs(u - v) > max_diff) continue;
+                    lab[q] = s;
+                    stack[top++] = q;
+                }
+            }
+            if (cnt <= max_size)
+                for (int i = 0; i < cnt; ++i) PX(region[i] % width, region[i] / width) = new_val;
+        }
+    }
+#undef PX
+    free(lab);
+    free(stack);
+    free(region);
+    return 0;
+}

@@ -107,6 +107,14 @@ int orc_matcher_compute(int width, int height, const orc_params* params,
                         float* conf, size_t conf_step,
                         const int* p2_lut);
 
+/* Speckle filter, sequential flood fill: the published semantics of OpenCV's
+ * cv::filterSpeckles (calib3d; the reference's bench/pyrsgm_bench.cpp:314
+ * passes it to StereoSGBM off).  4-neighbours join one region when neither
+ * equals new_val and |a - b| <= max_diff; regions of at most max_size pixels
+ * become new_val.  In place; step in bytes.  Returns 0 or -1. */
+int orc_filter_speckles(int16_t* img, size_t step, int width, int height, int16_t new_val, int max_size,
+                        int max_diff);
+
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int orc_num_threads(void);
 void orc_set_num_threads(int n);

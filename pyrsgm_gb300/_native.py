@@ -107,6 +107,7 @@ _SIGS = {
     "pyrsgm_gb300_read_pgm": (_i, [C.c_char_p, _vp, _sz, C.POINTER(_i), C.POINTER(_i), C.c_char_p, _sz]),
     "pyrsgm_gb300_write_pgm": (_i, [C.c_char_p, _vp, _sz, _i, _i, C.c_char_p, _sz]),
     "pyrsgm_gb300_read_ndisp": (_i, [C.c_char_p]),
+    "pyrsgm_gb300_filter_speckles": (_i, [_vp, _sz, _i, _i, C.c_short, _i, _i, _vp]),
     "pyrsgm_gb300_evaluate": (_i, [_vp, _sz, _vp, _sz, _vp, _sz, _i, _i, _f, C.POINTER(Metrics)]),
     "pyrsgm_gb300_profile": (_i, [_i]),
     "pyrsgm_gb300_profile_read": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),

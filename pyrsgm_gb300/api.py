@@ -190,6 +190,20 @@ class StereoMatcher:
         return out
 
 
+def filter_speckles(disp16: torch.Tensor, new_val: int, max_speckle_size: int, max_diff: int,
+                    stream=None) -> torch.Tensor:
+    """In place on an int16 device map: regions (4-neighbours differing by at
+    most max_diff, none equal to new_val) of at most max_speckle_size pixels
+    become new_val (cv::filterSpeckles semantics).  Returns disp16."""
+    if disp16.dtype != torch.int16 or disp16.dim() != 2 or not disp16.is_cuda:
+        raise ValueError("pyrsgm: filter_speckles takes a 2-D int16 CUDA tensor")
+    h, w = disp16.shape
+    if lib().pyrsgm_gb300_filter_speckles(_ptr(disp16), _pitch(disp16), w, h, int(new_val), int(max_speckle_size),
+                                          int(max_diff), _stream(stream)) != 0:
+        raise RuntimeError("pyrsgm: filter_speckles failed")
+    return disp16
+
+
 def set_packed_words(words: int) -> int:
     """Shape of the 16/32/64-label aggregation kernels (0 per launch, 8, or 2/4);
     returns the previous setting.  Results do not depend on it."""

@@ -63,6 +63,7 @@ def oracle() -> C.CDLL:
                                           _vp, _sz, _vp]
         h.orc_p2_table_libm.argtypes = [_i, _f, _f, _f, _f, _vp]
         h.orc_set_num_threads.argtypes = [_i]
+        h.orc_filter_speckles.argtypes = [_vp, _sz, _i, _i, C.c_short, _i, _i]
         _orc = h
     return _orc
 
@@ -78,6 +79,13 @@ def orc_pyrdown(src: np.ndarray) -> np.ndarray:
     r = oracle().orc_pyrdown_u8(_p(src), w, w, h, _p(dst), dst.shape[1], dst.shape[1], dst.shape[0])
     assert r == 0
     return dst
+
+
+def orc_speckles(img: np.ndarray, new_val: int, max_size: int, max_diff: int) -> np.ndarray:
+    out = np.ascontiguousarray(img, dtype=np.int16).copy()
+    h, w = out.shape
+    assert oracle().orc_filter_speckles(_p(out), w * 2, w, h, new_val, max_size, max_diff) == 0
+    return out
 
 
 def _lut_arg(lut):
