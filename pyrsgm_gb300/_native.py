@@ -112,6 +112,9 @@ _SIGS = {
     "pyrsgm_gb300_profile": (_i, [_i]),
     "pyrsgm_gb300_profile_read": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
 }
+# the Tri3SGM engine's names for the same two entry points (pyrsgm_tri3sgm.h)
+_SIGS["cuda_3sgm_compute_with_workspace"] = _SIGS["pyrsgm_compute_single_scale"]
+_SIGS["cuda_3sgm_compute_pyramid_level_with_workspace"] = _SIGS["pyrsgm_compute_level"]
 
 # Entry points declared in include/pyrsgm/*.h (checked by the tests).
 EXPORTS = tuple(_SIGS)

@@ -32,9 +32,12 @@
 // double-buffer the window and exchange it with one __syncwarp per step;
 // their minima reduce by __shfl_xor_sync.
 //
-// Loads: per thread a ring of kStages steps in shared memory filled with
-// cp.async (costs, label base, image byte), so the loads of a step are
-// issued kStages - 1 steps before it without holding registers.
+// Loads: rings in shared memory filled with cp.async, so the loads of a
+// step are issued several steps before it without holding registers.  The
+// T->B pass has one slot per step and thread (a warp's 32 columns are
+// adjacent, so its requests are whole lines already); the horizontal pass
+// of the NW = 8 shapes moves 128-byte runs of each chain with the whole
+// warp (chunk_steps), that of the spread shapes streams per lane.
 //
 // Paths: the T->B chains write their costs into V, the L->R and R->L chains
 // of each row into Vl and Vr; the chains never exchange data.  The WTA
@@ -61,8 +64,8 @@ constexpr uint32_t kOne2 = 0x00010001u;
 // many rows), 2 for the spread shapes (more, smaller blocks for few rows).
 template <int NW>
 __host__ __device__ constexpr int warps_of() { return NW == 8 ? 4 : 2; }
-constexpr int kStages = 6;       // look-ahead of the horizontal pass (steps)
 constexpr int kStagesTb = 8;     // look-ahead of the top->bottom pass
+constexpr int kStagesLane = 6;   // look-ahead of the per-lane horizontal pass
 
 __device__ __forceinline__ uint32_t dup(int v) { return ((uint32_t)v & 0xffffu) * 0x10001u; }
 
@@ -314,11 +317,31 @@ __device__ __forceinline__ void wta_out(const LevelDesc& J, int y, int x, int ba
     J.conf_raw[p] = cout;
 }
 
+// Horizontal pass I/O: CH steps of one chain are one 128-byte run of a
+// cost or path volume (D = 16: 4 pixels, 32: 2, 64: 1).  The warp moves
+// the runs of all its chains between global and shared memory together, 8
+// lanes per run, so every request is a whole 128-byte line: one 32-byte
+// stream per lane (a row and direction each) reaches about half the HBM
+// bandwidth of line requests.  SC chunk slots in flight per warp.
+template <int D>
+__host__ __device__ constexpr int chunk_steps() { return D >= 64 ? 1 : 64 / D; }
+template <int D>
+__host__ __device__ constexpr int chunk_stages() { return chunk_steps<D>() == 4 ? 3 : chunk_steps<D>() == 2 ? 4 : 6; }
+
 template <int NW, int T>
 constexpr size_t row_smem()
 {
     using G = Grp<NW, T>;
-    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + kStages * 32 * (G::RSW_TB + 2));
+    constexpr int CH = chunk_steps<G::D>(), SC = chunk_stages<G::D>();
+    // per warp: window buffers, SC input chunk slots and one output chunk
+    // (32 words per chain each), the label-base / image ring
+    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + (SC + 1) * G::CPW * 32 + SC * CH * 64);
+}
+template <int NW, int T>
+constexpr size_t row_lane_smem()
+{
+    using G = Grp<NW, T>;
+    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + kStagesLane * 32 * (G::RSW_TB + 2));
 }
 template <int NW, int T>
 constexpr size_t tb_smem()
@@ -423,13 +446,187 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_gtb(const __grid_co
 // and an R->L chain group of T threads.  Each chain walks its whole range
 // and stores its path costs (L->R into Vl, R->L into Vr); the chains of a
 // row never exchange data, and the WTA kernel adds the paths.
+//
+// Costs come in and path costs go out in chunks of CH steps per chain (one
+// 128-byte run each, chunk_steps): lane l of the warp moves 16-byte piece
+// l % 8 of the runs of chains 4j + l / 8 (j < CPW / 4), which all share one
+// direction ((l / 8) & 1) and so one step -> x mapping.  A chain's run sits
+// in 32 shared words with piece p at column p ^ (chain & 7), so that both
+// the line-wide copies and the per-chain reads of a step are free of bank
+// conflicts.
 // ---------------------------------------------------------------------------
 template <int NW, int T, bool PYR, int NJ>
 __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_constant__ Jobs<NJ> jobs)
 {
     using namespace pk;
     using G = Grp<NW, T>;
-    constexpr int D = G::D, RPW = G::CPW / 2, S = kStages, RS = G::RSW_TB, kWarps = warps_of<NW>();
+    constexpr int D = G::D, CPW = G::CPW, RPW = CPW / 2, kWarps = warps_of<NW>();
+    constexpr int CH = chunk_steps<D>(), SC = chunk_stages<D>();
+    constexpr int PPX = D / 8;          // 16-byte pieces per pixel
+    constexpr int NCOP = CPW / 4;       // pieces a lane moves per chunk
+    constexpr int SLOTW = CPW * 32;     // words of one chunk slot
+    const LevelDesc& J = jobs.d[blockIdx.y];
+    extern __shared__ __align__(16) uint32_t smem[];
+    int* lut = reinterpret_cast<int*>(smem);
+    uint32_t* cbuf = smem + 256;
+    uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
+    uint32_t* bibuf = rbuf + kWarps * (SC + 1) * SLOTW;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
+    for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = lane / T, k = lane % T, r = c >> 1, dir = c & 1;
+    const int row0 = (blockIdx.x * kWarps + warp) * RPW;
+    if (row0 >= J.h) return;   // the whole warp is past the image
+    const int y = row0 + r;
+    const int yy = imin(y, J.h - 1);
+    const int W = J.w, H = J.h;
+    uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
+    uint32_t* ring = rbuf + warp * (SC + 1) * SLOTW;
+    uint32_t* ob = ring + SC * SLOTW;
+    uint32_t* bi = bibuf + warp * SC * CH * 64 + lane;   // [slot][step][base, image][lane]
+
+    // path extents (single-scale: kernel_AggregateLR/RL ranges)
+    int lr_x0 = 0, lr_n, rl_n;
+    if (PYR) {
+        lr_n = J.paths >= 2 ? W : 0;
+        rl_n = W;
+    } else {
+        const int minX1 = imax(J.minD + D, 0), maxX1 = W + imin(J.minD, 0);
+        lr_x0 = minX1;
+        lr_n = J.paths >= 2 ? imax(0, maxX1 - minX1) : 0;
+        rl_n = imax(0, W - minX1);
+    }
+    const int Tn = imax(lr_n, rl_n);
+    const int n_mine = dir == 0 ? lr_n : rl_n;
+    const int dx = dir == 0 ? 1 : -1;
+    const int xs = dir == 0 ? lr_x0 : W - 1;   // step t of a chain is at x = xs + dx * t
+    const int16_t* const Cg = J.C;
+    const int16_t* const Bg = J.base;
+    const uint8_t* const Lg = J.left;
+    const bool use_base = PYR && J.refine, adaptive = J.adaptive != 0;
+    const int P2c = J.P2, minD = J.minD;
+    const size_t prow = (size_t)yy * W, lrow = (size_t)yy * J.lstep;
+
+    // this lane's share of the warp-wide chunk copies
+    const int pce = lane & 7, cdir = (lane >> 3) & 1, crow = row0 + (lane >> 4);
+    const int cq = pce / PPX, cs = cdir ? CH - 1 - cq : cq;   // pixel of the run, step of that pixel
+    const int cn = cdir ? rl_n : lr_n, cxs = cdir ? W - 1 : lr_x0, cdx = cdir ? -1 : 1;
+    const int coff = (pce % PPX) * 8;                          // int16 offset inside the pixel
+    int16_t* const Og = cdir ? J.Vr : J.Vl;
+    const size_t rstride = (size_t)2 * W * D;                  // two rows (chain 4j -> 4j + 4)
+    auto piece_col = [](int chn, int p) { return chn * 32 + ((p ^ (chn & 7)) << 2); };
+
+    int ci_issue = 0;
+    auto issue_next = [&](int slot) {
+        const int t = ci_issue * CH + cs;
+        if (t < cn) {
+            const size_t src = ((size_t)crow * W + (cxs + cdx * t)) * D + coff;
+#pragma unroll
+            for (int j = 0; j < NCOP; ++j)
+                if (crow + 2 * j < H)
+                    cp16(ring + slot * SLOTW + piece_col(4 * j + (lane >> 3), pce), Cg + src + j * rstride);
+        }
+#pragma unroll
+        for (int s = 0; s < CH; ++s) {
+            const int ts = ci_issue * CH + s;
+            if (ts < n_mine) {
+                const int x = xs + dx * ts;
+                if (use_base) cp4(bi + (slot * CH + s) * 64, word_of(Bg + prow + x));
+                if (adaptive) cp4(bi + (slot * CH + s) * 64 + 32, word_of(Lg + lrow + x));
+            }
+        }
+        cp_commit();
+        ++ci_issue;
+    };
+
+    const uint32_t p12 = dup(imin(J.P1, 0x8000));
+    GChain<NW> st;
+    gchain_init(st, minD);
+    const int NC = (Tn + CH - 1) / CH;
+#pragma unroll
+    for (int j = 0; j < SC - 1; ++j) issue_next(j);
+    int img_prev = 0, slot = 0, islot = SC - 1;
+    for (int ci = 0; ci < NC; ++ci) {
+        issue_next(islot);
+        islot = islot + 1 == SC ? 0 : islot + 1;
+        cp_wait<SC - 1>();
+        __syncwarp();
+        const uint32_t* cin = ring + slot * SLOTW;
+        const uint32_t* db = bi + slot * CH * 64;
+#pragma unroll
+        for (int s = 0; s < CH; ++s) {
+            const int t = ci * CH + s;
+            if (t >= Tn) break;   // the same for the whole warp
+            // this lane's NW words of step s: word q * D / 2 + k * NW of the run
+            const int q = dir ? CH - 1 - s : s;
+            const int w0 = q * (D / 2) + k * NW;
+            uint32_t cc[NW];
+            if constexpr (NW == 2) {
+                const uint2 a = *reinterpret_cast<const uint2*>(cin + piece_col(c, w0 >> 2) + (w0 & 3));
+                cc[0] = a.x; cc[1] = a.y;
+            } else {
+#pragma unroll
+                for (int i = 0; i < NW / 4; ++i) {
+                    const uint4 a = *reinterpret_cast<const uint4*>(cin + piece_col(c, (w0 >> 2) + i));
+                    cc[4 * i] = a.x; cc[4 * i + 1] = a.y; cc[4 * i + 2] = a.z; cc[4 * i + 3] = a.w;
+                }
+            }
+            const int x = xs + dx * t;
+            const int base = use_base ? (int)(int16_t)(db[s * 64] >> (((prow + x) & 1) * 16)) : minD;
+            int p2 = P2c;
+            if (adaptive) {
+                const int img = (int)((db[s * 64 + 32] >> byte_shift(Lg + lrow + x)) & 255u);
+                p2 = lut[abs(img - img_prev) & 255];
+                img_prev = img;
+            }
+            if (PYR && !J.refine) {
+                int lo, hi;
+                label_range(J, x, minD, lo, hi);
+                mask_labels<NW>(cc, lo, hi, k);
+            }
+            gstep<NW, T, PYR>(st, cc, base, p2, p12, chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0), k);
+            if constexpr (NW == 2) {
+                *reinterpret_cast<uint2*>(ob + piece_col(c, w0 >> 2) + (w0 & 3)) = make_uint2(st.L[0], st.L[1]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < NW / 4; ++i)
+                    *reinterpret_cast<uint4*>(ob + piece_col(c, (w0 >> 2) + i)) =
+                        make_uint4(st.L[4 * i], st.L[4 * i + 1], st.L[4 * i + 2], st.L[4 * i + 3]);
+            }
+        }
+        __syncwarp();
+        {
+            const int t = ci * CH + cs;
+            if (t < cn) {
+                const size_t dst = ((size_t)crow * W + (cxs + cdx * t)) * D + coff;
+#pragma unroll
+                for (int j = 0; j < NCOP; ++j)
+                    if (crow + 2 * j < H)
+                        *reinterpret_cast<uint4*>(Og + dst + j * rstride) =
+                            *reinterpret_cast<const uint4*>(ob + piece_col(4 * j + (lane >> 3), pce));
+            }
+        }
+        __syncwarp();
+        slot = slot + 1 == SC ? 0 : slot + 1;
+    }
+    cp_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// Horizontal paths, per-lane loads: the same chains as k_grow, each thread
+// streaming its own costs through a ring of kStagesLane steps and storing
+// its path costs directly.  For the spread shapes (NW < 8) on launches with
+// few rows, where the per-step latency of a chain bounds the pass rather
+// than HBM: the warp-wide chunk copies of k_grow add two warp
+// synchronisations and a shared-memory round trip to every chunk.
+// ---------------------------------------------------------------------------
+template <int NW, int T, bool PYR, int NJ>
+__global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow_lane(const __grid_constant__ Jobs<NJ> jobs)
+{
+    using namespace pk;
+    using G = Grp<NW, T>;
+    constexpr int D = G::D, RPW = G::CPW / 2, S = kStagesLane, RS = G::RSW_TB, kWarps = warps_of<NW>();
     const LevelDesc& J = jobs.d[blockIdx.y];
     extern __shared__ __align__(16) uint32_t smem[];
     int* lut = reinterpret_cast<int*>(smem);
@@ -662,15 +859,25 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * ((tbj.d[0].refine ? 2 : 0) + (tbj.d[0].adaptive ? 1 : 0)), tbst);
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
     }
-    constexpr size_t smem = pk::row_smem<NW, T>();
-    if ((err = cudaFuncSetAttribute(k_grow<NW, T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
-        return err;
     constexpr int kWarps = pk::warps_of<NW>();
     const int rows = kWarps * G::CPW / 2;
     dim3 g((e.max_h + rows - 1) / rows, jobs.n);
-    prof_begin(st);
-    k_grow<NW, T, PYR, NJ><<<g, kWarps * 32, smem, st>>>(jobs);
+    // NW == 8 (many rows): warp-wide 128-byte chunk I/O; spread shapes: per-lane streams
+    if constexpr (NW == 8) {
+        constexpr size_t smem = pk::row_smem<NW, T>();
+        if ((err = cudaFuncSetAttribute(k_grow<NW, T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem)) != cudaSuccess)
+            return err;
+        prof_begin(st);
+        k_grow<NW, T, PYR, NJ><<<g, kWarps * 32, smem, st>>>(jobs);
+    } else {
+        constexpr size_t smem = pk::row_lane_smem<NW, T>();
+        if ((err = cudaFuncSetAttribute(k_grow_lane<NW, T, PYR, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem)) != cudaSuccess)
+            return err;
+        prof_begin(st);
+        k_grow_lane<NW, T, PYR, NJ><<<g, kWarps * 32, smem, st>>>(jobs);
+    }
     count_launch();
     if (prof_enabled()) {
         // algorithmic bytes: each horizontal path reads the cost volume and

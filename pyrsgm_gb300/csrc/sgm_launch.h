@@ -15,7 +15,7 @@
 
 namespace pg {
 
-constexpr int kBatchJobs = 16;  // level jobs per batched launch
+constexpr int kBatchJobs = 64;  // level jobs per batched launch
 constexpr int kBatchPyr = 32;   // pyrDown images per batched launch
 
 struct PyrDownDesc {

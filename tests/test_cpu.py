@@ -115,10 +115,11 @@ def test_level_geometry_matches_oracle(w, h, kw):
 # --- C ABI: exports and argument checks (no device work) --------------------
 def _declared_functions() -> set[str]:
     names = set()
-    for hdr in ("pyrsgm_c.h", "pyrsgm_gb300.h", "pyrsgm_io.h"):
+    for hdr in sorted(os.listdir(os.path.join(ROOT, "include", "pyrsgm"))):
         text = open(os.path.join(ROOT, "include", "pyrsgm", hdr)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        names.update(re.findall(r"\b(pyrsgm_\w+)\s*\(", text))
+        text = re.sub(r"//[^\n]*", "", text)
+        names.update(re.findall(r"\b((?:pyrsgm|cuda_3sgm)_\w+)\s*\(", text))
     return names
 
 

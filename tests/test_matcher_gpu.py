@@ -176,3 +176,47 @@ def test_single_scale_entry(cost):
     assert r == 0
     torch.cuda.synchronize()
     assert _has_expected(d32, 32.0, 1.0)
+
+
+class _Tri3sgmNames:
+    """The library with the pyrsgm_c.h entry points replaced by their
+    Tri3SGM-engine names (pyrsgm_tri3sgm.h)."""
+
+    def __init__(self, lib):
+        self._lib = lib
+        self.pyrsgm_compute_single_scale = lib.cuda_3sgm_compute_with_workspace
+        self.pyrsgm_compute_level = lib.cuda_3sgm_compute_pyramid_level_with_workspace
+
+    def __getattr__(self, name):
+        return getattr(self._lib, name)
+
+
+def test_tri3sgm_entry_points_equal_the_c_api(monkeypatch):
+    from pyrsgm_gb300 import _native, api
+    L = torch.from_numpy(make_pattern(320, 128, 16, False)).cuda()
+    R = torch.from_numpy(make_pattern(320, 128, 16, True)).cuda()
+
+    def run():
+        ws = [pg.Workspace(), pg.Workspace()]
+        out = []
+        d16, d32, cf = (torch.zeros((128, 320), dtype=t, device="cuda") for t in (torch.int16, torch.float32,
+                                                                                   torch.float32))
+        assert pg.compute_single_scale(ws[0], L, R, d16, d32, cf, num_disparities=32) == 0
+        out += [d16.clone(), d32.clone(), cf.clone()]
+        pl, pr = L[::2, ::2].contiguous(), R[::2, ::2].contiguous()
+        p16, p32, pcf = (torch.zeros((64, 160), dtype=t, device="cuda") for t in (torch.int16, torch.float32,
+                                                                                  torch.float32))
+        assert pg.compute_level(ws[1], pl, pr, None, None, p16, p32, pcf, num_disparities=16, max_disparity=15) == 0
+        assert pg.compute_level(ws[0], L, R, p16, pcf, d16, d32, cf, num_disparities=16, max_disparity=31,
+                                refine=True) == 0
+        out += [p16, d16, d32, cf]
+        torch.cuda.synchronize()
+        for w in ws:
+            w.close()
+        return [t.cpu().numpy() for t in out]
+
+    want = run()
+    monkeypatch.setattr(api, "lib", lambda: _Tri3sgmNames(_native.lib()))
+    got = run()
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
