@@ -34,6 +34,12 @@ static std::atomic<int> g_packed_words{[] {
     return e ? std::atoi(e) : 0;
 }()};
 int packed_words_override() { return g_packed_words.load(std::memory_order_relaxed); }
+static const int g_packed_wps = [] {
+    const char* e = std::getenv("PYRSGM_GB300_PACKED_WPS");
+    const int v = e ? std::atoi(e) : 0;
+    return v > 0 && v <= 64 ? v : 1;
+}();
+int packed_min_warps_per_sm() { return g_packed_wps; }
 
 int sm_count()
 {

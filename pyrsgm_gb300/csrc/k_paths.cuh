@@ -767,7 +767,7 @@ inline int packed_nw(int D, long long rows)
     if (force == 8) return 8;
     if (force == 2 || force == 4) return small;
     const long long warps8 = rows * 2 * (D / 16) / 32;
-    return warps8 >= sm_count() ? 8 : small;
+    return warps8 >= (long long)packed_min_warps_per_sm() * sm_count() ? 8 : small;
 }
 
 template <bool PYR, int NJ>

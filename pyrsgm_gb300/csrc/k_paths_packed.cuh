@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
     uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
     uint32_t* ring = rbuf + warp * (SC + 1) * SLOTW;
     uint32_t* ob = ring + SC * SLOTW;
-    uint32_t* bi = bibuf + warp * SC * CH * 64 + lane;   // [slot][step][base, image][lane]
+    uint32_t* bi = bibuf + warp * SC * CH * 64 + lane;   // [slot][2 * CH words][lane]
 
     // path extents (single-scale: kernel_AggregateLR/RL ranges)
     int lr_x0 = 0, lr_n, rl_n;
@@ -527,13 +527,27 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
                 if (crow + 2 * j < H)
                     cp16(ring + slot * SLOTW + piece_col(4 * j + (lane >> 3), pce), Cg + src + j * rstride);
         }
+        // label bases and image bytes of this lane's own chain: [2 * CH][32]
+        // words per slot, bases first.  A whole 4-step run whose bases sit
+        // on a 4-byte boundary takes two word copies (pixel pairs), its
+        // image bytes one; otherwise each step copies the word holding it.
+        uint32_t* bslot = bi + slot * CH * 64;
+        const int t0 = ci_issue * CH, xlo = dir ? xs - t0 - (CH - 1) : xs + t0;
+        const bool full = CH == 4 && t0 + CH - 1 < n_mine;
+        const bool fb = full && (reinterpret_cast<uintptr_t>(Bg + prow + xlo) & 3) == 0;
+        const bool fi = full && (reinterpret_cast<uintptr_t>(Lg + lrow + xlo) & 3) == 0;
+        if (use_base && fb) {
+            cp4(bslot, Bg + prow + xlo);
+            cp4(bslot + 32, Bg + prow + xlo + 2);
+        }
+        if (adaptive && fi) cp4(bslot + CH * 32, Lg + lrow + xlo);
 #pragma unroll
         for (int s = 0; s < CH; ++s) {
-            const int ts = ci_issue * CH + s;
+            const int ts = t0 + s;
             if (ts < n_mine) {
                 const int x = xs + dx * ts;
-                if (use_base) cp4(bi + (slot * CH + s) * 64, word_of(Bg + prow + x));
-                if (adaptive) cp4(bi + (slot * CH + s) * 64 + 32, word_of(Lg + lrow + x));
+                if (use_base && !fb) cp4(bslot + s * 32, word_of(Bg + prow + x));
+                if (adaptive && !fi) cp4(bslot + (CH + s) * 32, word_of(Lg + lrow + x));
             }
         }
         cp_commit();
@@ -554,6 +568,10 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
         __syncwarp();
         const uint32_t* cin = ring + slot * SLOTW;
         const uint32_t* db = bi + slot * CH * 64;
+        const int t0 = ci * CH, xlo = dir ? xs - t0 - (CH - 1) : xs + t0;
+        const bool full = CH == 4 && t0 + CH - 1 < n_mine;
+        const bool fb = full && (reinterpret_cast<uintptr_t>(Bg + prow + xlo) & 3) == 0;
+        const bool fi = full && (reinterpret_cast<uintptr_t>(Lg + lrow + xlo) & 3) == 0;
 #pragma unroll
         for (int s = 0; s < CH; ++s) {
             const int t = ci * CH + s;
@@ -573,10 +591,14 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
                 }
             }
             const int x = xs + dx * t;
-            const int base = use_base ? (int)(int16_t)(db[s * 64] >> (((prow + x) & 1) * 16)) : minD;
+            int base = minD;
+            if (use_base)
+                base = fb ? (int)(int16_t)(db[(q >> 1) * 32] >> ((q & 1) * 16))
+                          : (int)(int16_t)(db[s * 32] >> (((prow + x) & 1) * 16));
             int p2 = P2c;
             if (adaptive) {
-                const int img = (int)((db[s * 64 + 32] >> byte_shift(Lg + lrow + x)) & 255u);
+                const int img = fi ? (int)((db[CH * 32] >> (q * 8)) & 255u)
+                                   : (int)((db[(CH + s) * 32] >> byte_shift(Lg + lrow + x)) & 255u);
                 p2 = lut[abs(img - img_prev) & 255];
                 img_prev = img;
             }

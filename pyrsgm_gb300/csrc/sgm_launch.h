@@ -99,6 +99,8 @@ struct ForkStreams {
 ForkStreams& fork_streams(cudaStream_t st);
 // 0 (choose per launch), 8, or 2/4: the packed kernels' words per thread.
 int packed_words_override();
+// Warps per SM the NW = 8 shape must fill before a launch takes it.
+int packed_min_warps_per_sm();
 
 // Count of kernel launches issued by this library (process-wide); a CUDA
 // graph replay counts the kernels it contains.

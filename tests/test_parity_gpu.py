@@ -103,3 +103,34 @@ def test_packed_shapes_match_reference(case, words):
         other = _runners.run_oracle(case, _runners.device_lut(case))
     bad = _runners.compare(mine, other)
     assert not bad, bad
+
+
+# Widths that are not a multiple of 4 and single-scale ranges that start
+# off a 4-pixel boundary: the horizontal pass then mixes whole-run and
+# per-step copies of the label bases and image bytes.
+ODD_PACKED = [
+    cases._lvl("lvl_bt_refine_w157_adaptive", 157, 61, 16, cases.BT, True, bs=5, adaptive=True, seed=11),
+    cases._lvl("lvl_census_refine_w93_adaptive", 93, 47, 16, cases.CENSUS, True, adaptive=True,
+               p2p=cases.P2_SMOKE, seed=12),
+    cases._lvl("lvl_census_refine_d32_w131", 131, 40, 32, cases.CENSUS, True, seed=13),
+    cases._ss("ss_bt_d16_w101_minD3_adaptive", 101, 40, 16, cases.BT, minD=3, adaptive=True, seed=14),
+    cases._ss("ss_census_d64_w199_minDneg", 199, 36, 64, cases.CENSUS, minD=-5, adaptive=True,
+              p2p=cases.P2_SMOKE, seed=15),
+]
+
+
+@pytest.mark.parametrize("words", [8, 2])
+@pytest.mark.parametrize("case", ODD_PACKED, ids=[c["name"] for c in ODD_PACKED])
+def test_packed_shapes_odd_widths_match_reference(case, words):
+    import pyrsgm_gb300 as pg
+    prev = pg.set_packed_words(words)
+    try:
+        mine = _runners.run_mine(case)
+    finally:
+        pg.set_packed_words(prev)
+    if _oracle.ref_available():
+        other = _runners.run_ref(case)
+    else:
+        other = _runners.run_oracle(case, _runners.device_lut(case))
+    bad = _runners.compare(mine, other)
+    assert not bad, bad
