@@ -126,6 +126,11 @@ void pyrsgm_gb300_batch_destroy(void* engine);
 int pyrsgm_gb300_batch_run(void* engine, const pyrsgm_gb300_pair* pairs, int num_pairs, int use_graph,
                            cudaStream_t stream, char* err, size_t err_len);
 size_t pyrsgm_gb300_batch_bytes_in_use(void* engine);
+/* Allocates now the pooled plans for `count` pairs of one shape (size and
+ * parameters), so that later runs with up to `count` such pairs allocate
+ * nothing; -1 with a message when the budget would be exceeded. */
+int pyrsgm_gb300_batch_reserve(void* engine, int width, int height, const pyrsgm_gb300_params* params, int count,
+                               cudaStream_t stream, char* err, size_t err_len);
 /* Device bytes one pair of this size and parameters occupies in a batch
  * engine (or a StereoMatcher); 0 for invalid parameters. */
 size_t pyrsgm_gb300_pair_bytes(int width, int height, const pyrsgm_gb300_params* params);
@@ -171,6 +176,11 @@ int pyrsgm_gb300_server_inject_failure(void* server, int batches);
  * reason in err.  Unregister only while no request using it is in flight;
  * the server unregisters what is left when destroyed. */
 int pyrsgm_gb300_server_register(void* server, void* host, size_t bytes, char* err, size_t err_len);
+/* The same reservation on every stream lane (returns when allocated): a
+ * server expecting bursts of one shape keeps that many plans per lane
+ * resident, so no request waits for a device allocation. */
+int pyrsgm_gb300_server_reserve(void* server, int width, int height, const pyrsgm_gb300_params* params, int count,
+                                char* err, size_t err_len);
 int pyrsgm_gb300_server_unregister(void* server, void* host);
 
 /* out[7] = level, width, height, num_labels, max_disparity, block_size, refine */
@@ -202,6 +212,29 @@ int pyrsgm_gb300_filter_speckles(short* d_disp, size_t pitch_bytes, int width, i
  * setting, or -1 for another value.  The environment variable
  * PYRSGM_GB300_PACKED_NW gives the initial setting. */
 int pyrsgm_gb300_set_packed_words(int words);
+
+/* Measuring choice of that shape (off by default; the environment variable
+ * PYRSGM_GB300_AUTOTUNE=1 turns it on at load).  When on, the first run of
+ * a new batch in the batch engine (before its CUDA graph is captured)
+ * times both shapes for every aggregation launch whose key -- label count,
+ * pyramid mode, total rows, widest level -- has no entry yet, and records
+ * the faster; later launches with that key use it.  Timing synchronises
+ * the host with the stream, once per new key.  A forced shape
+ * (pyrsgm_gb300_set_packed_words) takes precedence.  Returns the previous
+ * setting. */
+int pyrsgm_gb300_set_autotune(int on);
+
+typedef struct {
+    int num_labels, pyramid, rows, width;  /* key */
+    int words;                             /* chosen words per thread (8, or 2/4) */
+    float ms_wide, ms_spread;              /* best time of each shape */
+} pyrsgm_gb300_tune_entry;
+
+/* Copies up to `capacity` recorded entries to `out` (may be NULL) and
+ * returns how many there are. */
+int pyrsgm_gb300_autotune_entries(pyrsgm_gb300_tune_entry* out, int capacity);
+/* Forgets every entry. */
+void pyrsgm_gb300_autotune_clear(void);
 
 /* Per-kernel profiling with CUDA events recorded on each launch's stream.
  * pyrsgm_gb300_profile(1) clears the records and starts recording,

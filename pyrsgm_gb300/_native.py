@@ -36,6 +36,12 @@ class Pair(C.Structure):
                 ("d_conf", _vp), ("conf_pitch", _sz), ("width", _i), ("height", _i), ("params", Params)]
 
 
+class TuneEntry(C.Structure):
+    """pyrsgm_gb300_tune_entry (include/pyrsgm/pyrsgm_gb300.h)."""
+    _fields_ = [("num_labels", C.c_int), ("pyramid", C.c_int), ("rows", C.c_int), ("width", C.c_int),
+                ("words", C.c_int), ("ms_wide", C.c_float), ("ms_spread", C.c_float)]
+
+
 class Metrics(C.Structure):
     """pyrsgm_gb300_metrics: disparity metrics against ground truth."""
     _fields_ = [("evaluated", _i), ("valid", _i)] + [(n, C.c_double) for n in (
@@ -88,6 +94,7 @@ _SIGS = {
     "pyrsgm_gb300_batch_destroy": (None, [_vp]),
     "pyrsgm_gb300_batch_run": (_i, [_vp, C.POINTER(Pair), _i, _i, _vp, C.c_char_p, _sz]),
     "pyrsgm_gb300_batch_bytes_in_use": (_sz, [_vp]),
+    "pyrsgm_gb300_batch_reserve": (_i, [_vp, _i, _i, C.POINTER(Params), _i, _vp, C.c_char_p, _sz]),
     "pyrsgm_gb300_pair_bytes": (_sz, [_i, _i, C.POINTER(Params)]),
     "pyrsgm_gb300_server_create": (_vp, [_sz, _i, _i, _i, C.c_char_p, _sz]),
     "pyrsgm_gb300_server_destroy": (None, [_vp]),
@@ -99,9 +106,13 @@ _SIGS = {
     "pyrsgm_gb300_server_inject_failure": (_i, [_vp, _i]),
     "pyrsgm_gb300_server_register": (_i, [_vp, _vp, _sz, C.c_char_p, _sz]),
     "pyrsgm_gb300_server_unregister": (_i, [_vp, _vp]),
+    "pyrsgm_gb300_server_reserve": (_i, [_vp, _i, _i, C.POINTER(Params), _i, C.c_char_p, _sz]),
     "pyrsgm_gb300_version": (C.c_char_p, []),
     "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
     "pyrsgm_gb300_set_packed_words": (_i, [_i]),
+    "pyrsgm_gb300_set_autotune": (_i, [_i]),
+    "pyrsgm_gb300_autotune_entries": (_i, [_vp, _i]),
+    "pyrsgm_gb300_autotune_clear": (None, []),
     "pyrsgm_gb300_read_pfm": (_i, [C.c_char_p, _vp, _sz, C.POINTER(_i), C.POINTER(_i), C.c_char_p, _sz]),
     "pyrsgm_gb300_write_pfm": (_i, [C.c_char_p, _vp, _sz, _i, _i, C.c_char_p, _sz]),
     "pyrsgm_gb300_read_pgm": (_i, [C.c_char_p, _vp, _sz, C.POINTER(_i), C.POINTER(_i), C.c_char_p, _sz]),

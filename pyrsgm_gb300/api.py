@@ -213,6 +213,27 @@ def set_packed_words(words: int) -> int:
     return r
 
 
+def set_autotune(on: bool) -> bool:
+    """Measure the 16/32/64-label kernel shape per launch key on the batch
+    engine's first run of each new batch (pyrsgm_gb300_set_autotune);
+    returns the previous setting."""
+    return bool(lib().pyrsgm_gb300_set_autotune(1 if on else 0))
+
+
+def autotune_table() -> list[dict]:
+    """Recorded shape choices: key (labels, pyramid, rows, width), chosen
+    words per thread and the best time of each shape in ms."""
+    n = lib().pyrsgm_gb300_autotune_entries(None, 0)
+    arr = (_native.TuneEntry * max(n, 1))()
+    n = min(n, lib().pyrsgm_gb300_autotune_entries(C.cast(arr, C.c_void_p), n))
+    return [{f: (round(getattr(arr[i], f), 4) if f.startswith("ms") else getattr(arr[i], f))
+             for f, _ in _native.TuneEntry._fields_} for i in range(n)]
+
+
+def autotune_clear() -> None:
+    lib().pyrsgm_gb300_autotune_clear()
+
+
 def pair_bytes(width: int, height: int, params: Params) -> int:
     """Device bytes one pair of this shape occupies (StereoMatcher or batch slot)."""
     return lib().pyrsgm_gb300_pair_bytes(width, height, C.byref(params.to_c()))
@@ -233,6 +254,13 @@ class BatchEngine:
 
     def bytes_in_use(self) -> int:
         return lib().pyrsgm_gb300_batch_bytes_in_use(self._h)
+
+    def reserve(self, width: int, height: int, params: Params, count: int, stream=None) -> None:
+        """Allocate now the plans for `count` pairs of this shape (pyrsgm_gb300_batch_reserve)."""
+        err = C.create_string_buffer(256)
+        if lib().pyrsgm_gb300_batch_reserve(self._h, width, height, C.byref(params.to_c()), count, _stream(stream),
+                                            err, 256) != 0:
+            raise RuntimeError(err.value.decode())
 
     @staticmethod
     def make_pairs(items: list[dict]):
@@ -329,6 +357,13 @@ class Server:
 
     def inject_failure(self, batches: int) -> None:
         lib().pyrsgm_gb300_server_inject_failure(self._h, batches)
+
+    def reserve(self, width: int, height: int, params: Params, count: int) -> None:
+        """Keep plans for `count` pairs of this shape resident on every lane
+        (pyrsgm_gb300_server_reserve)."""
+        err = C.create_string_buffer(256)
+        if lib().pyrsgm_gb300_server_reserve(self._h, width, height, C.byref(params.to_c()), count, err, 256) != 0:
+            raise RuntimeError(err.value.decode())
 
     def register(self, arr) -> bool:
         """Page-lock a numpy array the caller reuses for images or outputs, so

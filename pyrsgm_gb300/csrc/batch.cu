@@ -129,6 +129,25 @@ public:
 
     size_t bytesInUse() const { return used_; }
 
+    // Pooled plans for `count` pairs of one shape, allocated now, so that
+    // later runs with up to `count` such pairs allocate nothing.
+    void reserve(int w, int h, const pyrsgm::Params& p, int count, cudaStream_t st)
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (w <= 0 || h <= 0 || count < 0) throw std::invalid_argument("pyrsgm: bad reserve request");
+        const pyrsgm::Params v = pyrsgm::validateParams(p);
+        const ShapeKey k = keyOf(w, h, v);
+        auto& vec = pool_[k];
+        const size_t each = PairPlan::bytesFor(w, h, v);
+        while ((int)vec.size() < count) {
+            if (used_ + each > budget_)
+                throw std::runtime_error("pyrsgm batch: device-memory budget exceeded (" +
+                                         std::to_string(used_ + each) + " > " + std::to_string(budget_) + " bytes)");
+            vec.emplace_back(new PairPlan(w, h, v, st));
+            used_ += vec.back()->arena_bytes;
+        }
+    }
+
     void run(const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph)
     {
         std::lock_guard<std::mutex> lk(mu_);
@@ -159,8 +178,17 @@ public:
             if (cs != cudaStreamCaptureStatusNone) use_graph = false;  // caller is capturing: just enqueue
         }
         if (!use_graph) {
+            // measures unknown shape keys unless the stream is being captured
+            TuningScope scope;
             enqueue(pairs, plans, n, st);
             return;
+        }
+        if (autotune_enabled()) {
+            // first run of this batch: measure the kernel shapes of its
+            // aggregation launches (outputs are complete either way), then
+            // capture with the choices recorded
+            TuningScope scope;
+            enqueue(pairs, plans, n, st);
         }
         cudaGraph_t g = nullptr;
         check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -336,6 +364,10 @@ void batch_engine_run(BatchEngine* e, const pyrsgm_gb300_pair* pairs, int n, cud
 {
     e->run(pairs, n, st, use_graph);
 }
+void batch_engine_reserve(BatchEngine* e, int w, int h, const pyrsgm::Params& p, int count, cudaStream_t st)
+{
+    e->reserve(w, h, p, count, st);
+}
 
 }  // namespace pg
 
@@ -369,6 +401,19 @@ int pyrsgm_gb300_batch_run(void* engine, const pyrsgm_gb300_pair* pairs, int num
     if (!engine || (num_pairs > 0 && !pairs)) return -1;
     try {
         static_cast<pg::BatchEngine*>(engine)->run(pairs, num_pairs, stream, use_graph != 0);
+        return 0;
+    } catch (const std::exception& e) {
+        setErr(err, err_len, e.what());
+        return -1;
+    }
+}
+
+int pyrsgm_gb300_batch_reserve(void* engine, int width, int height, const pyrsgm_gb300_params* params, int count,
+                               cudaStream_t stream, char* err, size_t err_len)
+{
+    if (!engine || !params) return -1;
+    try {
+        static_cast<pg::BatchEngine*>(engine)->reserve(width, height, pg::toParams(*params), count, stream);
         return 0;
     } catch (const std::exception& e) {
         setErr(err, err_len, e.what());

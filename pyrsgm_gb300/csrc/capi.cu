@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <new>
 #include <utility>
 
@@ -40,6 +41,31 @@ static const int g_packed_wps = [] {
     return v > 0 && v <= 64 ? v : 1;
 }();
 int packed_min_warps_per_sm() { return g_packed_wps; }
+
+static std::atomic<int> g_autotune{[] {
+    const char* e = std::getenv("PYRSGM_GB300_AUTOTUNE");
+    return e && std::atoi(e) != 0 ? 1 : 0;
+}()};
+static thread_local bool t_tuning = false;
+static std::mutex g_tune_mu;
+static std::map<TuneKey, TuneEntry> g_tune;
+bool autotune_enabled() { return g_autotune.load(std::memory_order_relaxed) != 0; }
+bool tuning_thread() { return t_tuning; }
+TuningScope::TuningScope() : prev(t_tuning) { t_tuning = true; }
+TuningScope::~TuningScope() { t_tuning = prev; }
+bool tune_lookup(const TuneKey& k, TuneEntry& out)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(k);
+    if (it == g_tune.end()) return false;
+    out = it->second;
+    return true;
+}
+void tune_store(const TuneKey& k, const TuneEntry& e)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[k] = e;
+}
 
 int sm_count()
 {
@@ -395,6 +421,33 @@ int pyrsgm_gb300_set_packed_words(int words)
 {
     if (words != 0 && words != 2 && words != 4 && words != 8) return -1;
     return pg::g_packed_words.exchange(words, std::memory_order_relaxed);
+}
+
+int pyrsgm_gb300_set_autotune(int on) { return pg::g_autotune.exchange(on ? 1 : 0, std::memory_order_relaxed); }
+
+int pyrsgm_gb300_autotune_entries(pyrsgm_gb300_tune_entry* out, int capacity)
+{
+    std::lock_guard<std::mutex> lk(pg::g_tune_mu);
+    int n = 0;
+    for (const auto& kv : pg::g_tune) {
+        if (out && n < capacity) {
+            out[n].num_labels = kv.first.D;
+            out[n].pyramid = kv.first.pyr;
+            out[n].rows = kv.first.rows;
+            out[n].width = kv.first.w;
+            out[n].words = kv.second.nw;
+            out[n].ms_wide = kv.second.ms_wide;
+            out[n].ms_spread = kv.second.ms_spread;
+        }
+        ++n;
+    }
+    return n;
+}
+
+void pyrsgm_gb300_autotune_clear(void)
+{
+    std::lock_guard<std::mutex> lk(pg::g_tune_mu);
+    pg::g_tune.clear();
 }
 
 }  // extern "C"

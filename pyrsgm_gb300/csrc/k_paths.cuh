@@ -36,6 +36,9 @@
 // array directly.
 #pragma once
 
+#include <algorithm>
+#include <climits>
+
 #include "profiler.h"
 #include "sgm_common.cuh"
 #include "sgm_launch.h"
@@ -770,22 +773,79 @@ inline int packed_nw(int D, long long rows)
     return warps8 >= (long long)packed_min_warps_per_sm() * sm_count() ? 8 : small;
 }
 
+// Words per thread for a packed launch: a forced setting, else a recorded
+// measurement for its key, else (measuring it now when the thread is in a
+// tuning scope) the rule of packed_nw().  `run(nw)` launches one shape.
+template <class Run>
+int packed_choice(const TuneKey& key, long long rows, cudaStream_t st, Run run, cudaError_t& err)
+{
+    err = cudaSuccess;
+    if (packed_words_override() != 0 || !autotune_enabled()) return packed_nw(key.D, rows);
+    TuneEntry te;
+    if (tune_lookup(key, te)) return te.nw;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (!tuning_thread() || cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return packed_nw(key.D, rows);
+    const int spread = key.D == 64 ? 4 : 2;
+    float best[2] = {1e30f, 1e30f};
+    cudaEvent_t a = nullptr, b = nullptr;
+    if ((err = cudaEventCreate(&a)) != cudaSuccess || (err = cudaEventCreate(&b)) != cudaSuccess) {
+        if (a) cudaEventDestroy(a);
+        return packed_nw(key.D, rows);
+    }
+    for (int rep = 0; rep < 2 && err == cudaSuccess; ++rep) {
+        for (int c = 0; c < 2 && err == cudaSuccess; ++c) {
+            float ms = 0.0f;
+            if ((err = cudaEventRecord(a, st)) != cudaSuccess || (err = run(c == 0 ? 8 : spread)) != cudaSuccess ||
+                (err = cudaEventRecord(b, st)) != cudaSuccess || (err = cudaEventSynchronize(b)) != cudaSuccess ||
+                (err = cudaEventElapsedTime(&ms, a, b)) != cudaSuccess)
+                break;
+            best[c] = std::min(best[c], ms);
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (err != cudaSuccess) return packed_nw(key.D, rows);
+    te.nw = best[0] <= best[1] ? 8 : spread;
+    te.ms_wide = best[0];
+    te.ms_spread = best[1];
+    tune_store(key, te);
+    return te.nw;
+}
+
 template <bool PYR, int NJ>
 cudaError_t launch_paths_mode(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
     long long rows = 0;
     for (int i = 0; i < jobs.n; ++i) rows += jobs.d[i].h;
     const int D = jobs.d[0].D;
+    const TuneKey key{D, PYR ? 1 : 0, (int)std::min<long long>(rows, INT_MAX), e.max_w};
+    cudaError_t err = cudaSuccess;
     switch (path_variant(D)) {
-    case 10016:
-        return packed_nw(D, rows) == 8 ? launch_paths_packed<8, 1, PYR, NJ>(jobs, e, st)
-                                       : launch_paths_packed<2, 4, PYR, NJ>(jobs, e, st);
-    case 10032:
-        return packed_nw(D, rows) == 8 ? launch_paths_packed<8, 2, PYR, NJ>(jobs, e, st)
-                                       : launch_paths_packed<2, 8, PYR, NJ>(jobs, e, st);
-    case 10064:
-        return packed_nw(D, rows) == 8 ? launch_paths_packed<8, 4, PYR, NJ>(jobs, e, st)
-                                       : launch_paths_packed<4, 8, PYR, NJ>(jobs, e, st);
+    case 10016: {
+        auto run = [&](int nw) {
+            return nw == 8 ? launch_paths_packed<8, 1, PYR, NJ>(jobs, e, st)
+                           : launch_paths_packed<2, 4, PYR, NJ>(jobs, e, st);
+        };
+        const int nw = packed_choice(key, rows, st, run, err);
+        return err != cudaSuccess ? err : run(nw);
+    }
+    case 10032: {
+        auto run = [&](int nw) {
+            return nw == 8 ? launch_paths_packed<8, 2, PYR, NJ>(jobs, e, st)
+                           : launch_paths_packed<2, 8, PYR, NJ>(jobs, e, st);
+        };
+        const int nw = packed_choice(key, rows, st, run, err);
+        return err != cudaSuccess ? err : run(nw);
+    }
+    case 10064: {
+        auto run = [&](int nw) {
+            return nw == 8 ? launch_paths_packed<8, 4, PYR, NJ>(jobs, e, st)
+                           : launch_paths_packed<4, 8, PYR, NJ>(jobs, e, st);
+        };
+        const int nw = packed_choice(key, rows, st, run, err);
+        return err != cudaSuccess ? err : run(nw);
+    }
     case 1601: return launch_paths_shape<16, 1, PYR, NJ>(jobs, e, st);
     case 3201: return launch_paths_shape<32, 1, PYR, NJ>(jobs, e, st);
     case 3202: return launch_paths_shape<32, 2, PYR, NJ>(jobs, e, st);

@@ -109,6 +109,7 @@ class BatchEngine;
 BatchEngine* batch_engine_new(size_t budget);
 void batch_engine_delete(BatchEngine* e);
 void batch_engine_run(BatchEngine* e, const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph);
+void batch_engine_reserve(BatchEngine* e, int w, int h, const pyrsgm::Params& p, int count, cudaStream_t st);
 
 struct Lane {
     cudaStream_t st = nullptr;
@@ -265,6 +266,23 @@ public:
 
     // Page-lock a host range so that requests whose images or outputs lie
     // inside it are copied without staging.
+    // Plans for `count` pairs of one shape on every lane (allocated now;
+    // each lane's engine serialises this with its runs).
+    int reserve(int w, int h, const pyrsgm_gb300_params& prm, int count, std::string& err)
+    {
+        try {
+            const pyrsgm::Params p = toParams(prm);
+            for (auto& l : lanes_) {
+                batch_engine_reserve(l->eng, w, h, p, count, l->st);
+                if (cudaStreamSynchronize(l->st) != cudaSuccess) throw std::runtime_error("reserve: stream error");
+            }
+            return 0;
+        } catch (const std::exception& e) {
+            err = e.what();
+            return -1;
+        }
+    }
+
     int register_host(void* p, size_t bytes, std::string& err)
     {
         if (!p || bytes == 0) {
@@ -605,6 +623,19 @@ int pyrsgm_gb300_server_register(void* s, void* host, size_t bytes, char* err, s
     }
     std::string e;
     const int r = static_cast<pg::Server*>(s)->register_host(host, bytes, e);
+    if (r != 0) setErr(err, err_len, e);
+    return r;
+}
+
+int pyrsgm_gb300_server_reserve(void* s, int width, int height, const pyrsgm_gb300_params* params, int count,
+                                char* err, size_t err_len)
+{
+    if (!s || !params) {
+        setErr(err, err_len, "null server or params");
+        return -1;
+    }
+    std::string e;
+    const int r = static_cast<pg::Server*>(s)->reserve(width, height, *params, count, e);
     if (r != 0) setErr(err, err_len, e);
     return r;
 }

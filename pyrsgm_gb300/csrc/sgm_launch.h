@@ -102,6 +102,37 @@ int packed_words_override();
 // Warps per SM the NW = 8 shape must fill before a launch takes it.
 int packed_min_warps_per_sm();
 
+// Measuring shape choice for the 16/32/64-label aggregation (opt-in,
+// pyrsgm_gb300_set_autotune).  A launch is keyed by its label count, mode,
+// total rows and widest level; while the calling thread is in a tuning
+// scope (the batch engine's first, uncaptured run of a new batch) a key
+// without an entry times both kernel shapes on the launch stream (twice
+// each, host-synchronising; the outputs of either are identical) and keeps
+// the faster.  Outside a tuning scope a recorded entry is used and an
+// unknown key falls back to the rule of packed_nw().
+struct TuneKey {
+    int D, pyr, rows, w;
+    bool operator<(const TuneKey& o) const
+    {
+        return D != o.D ? D < o.D : pyr != o.pyr ? pyr < o.pyr : rows != o.rows ? rows < o.rows : w < o.w;
+    }
+};
+struct TuneEntry {
+    int nw;              // chosen words per thread
+    float ms_wide;       // NW = 8 shape, best of two
+    float ms_spread;     // spread shape (NW = 2, or 4 for 64 labels), best of two
+};
+bool autotune_enabled();
+bool tuning_thread();
+// RAII: marks the calling thread as allowed to measure.
+struct TuningScope {
+    TuningScope();
+    ~TuningScope();
+    bool prev;
+};
+bool tune_lookup(const TuneKey& k, TuneEntry& out);
+void tune_store(const TuneKey& k, const TuneEntry& e);
+
 // Count of kernel launches issued by this library (process-wide); a CUDA
 // graph replay counts the kernels it contains.
 void count_launch();

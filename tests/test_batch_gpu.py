@@ -114,3 +114,39 @@ def test_batch_rejects_invalid_params():
         eng.run([dict(left=L, right=L, params=pg.Params(pyramid_levels=7),
                       disp16=torch.zeros((48, 64), dtype=torch.int16, device="cuda"))])
     eng.close()
+
+
+def test_autotuned_batch_matches_each_pair_alone():
+    """With the measuring shape choice on, the first run of a batch times
+    both shapes of every 16/32/64-label aggregation launch, records the
+    faster, and the captured graph uses it; results are unchanged."""
+    prev = pg.set_autotune(True)
+    pg.autotune_clear()
+    try:
+        batch = mixed_batch(12, seed=4700)
+        eng = pg.BatchEngine(8 << 30)
+        st = torch.cuda.Stream()
+        items, dev = [], []
+        for p, left, right, want in batch:
+            h, w = left.shape
+            o = _alloc(h, w, want)
+            items.append(dict(left=torch.from_numpy(left).cuda(), right=torch.from_numpy(right).cuda(), params=p, **o))
+            dev.append(o)
+        torch.cuda.synchronize()
+        for _ in range(2):   # tuning run + capture, then a replay
+            eng.run(items, use_graph=True, stream=st)
+        torch.cuda.synchronize()
+        table = pg.autotune_table()
+        assert table, "no shape was measured"
+        for t in table:
+            assert t["num_labels"] in (16, 32, 64) and t["rows"] > 0 and t["width"] > 0
+            assert t["words"] in (8, 4 if t["num_labels"] == 64 else 2)
+            assert t["ms_wide"] > 0 and t["ms_spread"] > 0
+            assert (t["words"] == 8) == (t["ms_wide"] <= t["ms_spread"])
+        for i, (p, left, right, want) in enumerate(batch):
+            got = {k: (v.cpu().numpy() if v is not None else None) for k, v in dev[i].items()}
+            _check(got, _alone(p, left, right, want), f"pair {i}")
+        eng.close()
+    finally:
+        pg.set_autotune(prev)
+        pg.autotune_clear()

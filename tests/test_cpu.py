@@ -202,3 +202,14 @@ def test_oracle_matches_reference_golden(case):
 def test_oracle_pyrdown_matches_reference_golden(w, h):
     g = _golden()
     np.testing.assert_array_equal(_oracle.orc_pyrdown(cases.pyrdown_input(w, h)), g[f"pyrdown_{w}x{h}"])
+
+
+def test_autotune_switch_and_empty_table_without_device_work():
+    import pyrsgm_gb300 as pg
+    prev = pg.set_autotune(True)
+    try:
+        assert pg.set_autotune(True) is True
+        pg.autotune_clear()
+        assert pg.autotune_table() == []
+    finally:
+        pg.set_autotune(prev)

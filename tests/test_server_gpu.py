@@ -148,3 +148,38 @@ def test_registered_buffers_are_copied_in_place():
         np.testing.assert_allclose(out["disp32"], ref["disp32"], atol=1e-6, rtol=0)
         np.testing.assert_allclose(out["conf"], ref["conf"], atol=1e-6, rtol=0)
     srv.close()
+
+
+def test_reserved_plans_serve_bursts_without_allocation():
+    """Plans reserved up front on every lane: a burst of that shape runs on
+    them and gives the results of each pair alone; a reservation beyond a
+    lane's budget is refused."""
+    p = pg.Params(num_disparities=64, pyramid_levels=1, cost_mode=pg.COST_CENSUS, p1=8, p2=32)
+    w, h = 160, 96
+    one = pg.pair_bytes(w, h, p)
+    srv = pg.Server(64 * one, max_batch=4, streams=2)
+    srv.reserve(w, h, p, 4)
+    reqs = [synth.make_pair(w, h, 40, 5, 6500 + i)[:2] for i in range(8)]
+    ids = [srv.submit(l, r, p, True, True, True) for l, r in reqs]
+    for (l, r), (rid, out) in zip(reqs, ids):
+        assert srv.wait(rid, 60.0) == 1
+        want = _alone(p, l, r)
+        np.testing.assert_array_equal(out["disp16"], want["disp16"])
+        np.testing.assert_allclose(out["conf"], want["conf"], rtol=0, atol=1e-6)
+    with pytest.raises(RuntimeError, match="budget"):
+        srv.reserve(w, h, p, 40)   # 40 plans per lane > a lane's 32-plan budget
+    srv.close()
+
+
+def test_batch_reserve_allocates_plans_up_front():
+    p = pg.Params(num_disparities=64, pyramid_levels=1)
+    one = pg.pair_bytes(160, 96, p)
+    eng = pg.BatchEngine(8 * one)
+    eng.reserve(160, 96, p, 3)
+    assert eng.bytes_in_use() == 3 * one
+    eng.reserve(160, 96, p, 2)   # already there
+    assert eng.bytes_in_use() == 3 * one
+    with pytest.raises(RuntimeError, match="budget"):
+        eng.reserve(160, 96, p, 9)
+    assert eng.bytes_in_use() == 8 * one   # filled up to the budget before refusing
+    eng.close()
