@@ -84,9 +84,14 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once nvidia-smi is sampling
+            t_end = time.time() + 5.0
+            while not self.lines and time.time() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.skip = len(self.lines)
         except OSError:
             self.proc = None
         return self
@@ -108,7 +113,7 @@ class ClockSampler:
     def summary(self) -> dict:
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[getattr(self, "skip", 0):]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 8:
                 continue
@@ -403,19 +408,21 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(1)
-                ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.batch + 1)]
-                ev[0].record(stream)
-                runner.step(stream, ev[1:] if pair_timing else None)
-                if not pair_timing:
-                    ev[-1].record(stream)
-            torch.cuda.synchronize()
-            step_ms.append(ev[0].elapsed_time(ev[-1]))
-            if pair_timing:
-                pair_ms += [ev[i].elapsed_time(ev[i + 1]) for i in range(args.batch)]
+    # clocks are sampled from here to the end of the e2e runs
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.__enter__()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.batch + 1)]
+            ev[0].record(stream)
+            runner.step(stream, ev[1:] if pair_timing else None)
+            if not pair_timing:
+                ev[-1].record(stream)
+        torch.cuda.synchronize()
+        step_ms.append(ev[0].elapsed_time(ev[-1]))
+        if pair_timing:
+            pair_ms += [ev[i].elapsed_time(ev[i + 1]) for i in range(args.batch)]
     torch.cuda.synchronize()
     launches = runner.launches() - n0
     prof = {}
@@ -471,6 +478,7 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
                 b.record(stream)
             torch.cuda.synchronize()
             e2e_ms.append(a.elapsed_time(b))
+    clk.__exit__(None, None, None)
     e2e_total = sum(e2e_ms)
     if world > 1:
         t = torch.tensor([total_ms, e2e_total], device=dev)
@@ -524,7 +532,7 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
         counts[key] = counts.get(key, 0) + 1
     for key, cnt in counts.items():
         try:
-            srv.reserve(key[0], key[1], params_of(key[2]), min(max_batch, cnt))
+            srv.reserve(key[0], key[1], params_of(key[2]), min(max_batch, 2 * cnt))
         except RuntimeError:   # the lanes' budget is full: later shapes allocate on first use
             break
     for rep in range(2):

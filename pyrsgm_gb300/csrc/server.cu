@@ -7,9 +7,10 @@
 // copies the inputs through pinned staging, runs the lane's batch engine and
 // copies the outputs back, all asynchronously on the lane's stream; while
 // one lane's batch is on the GPU the next lane takes the requests that
-// arrived meanwhile, so batches overlap on the device.  A completion thread
-// waits for each lane's event in order, hands the results to the callers'
-// buffers and records the latency (submit -> results in host memory).
+// arrived meanwhile, so batches overlap on the device.  Each lane has a
+// completion thread that waits for its lane's event, hands the results to
+// the callers' buffers, records the latency (submit -> results in host
+// memory) and frees the lane, independently of the other lanes.
 //
 // Host buffers that the caller registered (pyrsgm_gb300_server_register,
 // page-locked with cudaHostRegister) are copied by DMA directly; other
@@ -119,7 +120,8 @@ struct Lane {
     std::vector<Request*> reqs;
     std::vector<IOBuf*> bufs;
     std::vector<void*> staged;   // per request and output: staging used (null: copied in place or absent)
-    bool busy = false;
+    bool busy = false;       // a batch is assigned to the lane and not yet finished
+    bool launched = false;   // that batch is enqueued; the lane's completion thread takes it
     std::string error;  // set when the batch failed before reaching the GPU
 };
 
@@ -139,7 +141,9 @@ public:
             lanes_.push_back(std::move(L));
         }
         sched_ = std::thread([this] { schedule(); });
-        comp_ = std::thread([this] { complete(); });
+        // one completion thread per lane: a lane is free again as soon as its
+        // own batch is done, whatever the other lanes are running
+        for (auto& L : lanes_) comps_.emplace_back([this, l = L.get()] { complete(*l); });
     }
 
     ~Server()
@@ -150,7 +154,7 @@ public:
         }
         cv_.notify_all();
         sched_.join();
-        comp_.join();
+        for (auto& t : comps_) t.join();
         for (auto& L : lanes_) {
             cudaStreamSynchronize(L->st);
             for (auto& kv : L->pool)
@@ -411,7 +415,7 @@ private:
             cudaEventRecord(L->done, L->st);
             {
                 std::lock_guard<std::mutex> lk(mu_);
-                pending_.push_back(L);
+                L->launched = true;
             }
             cv_.notify_all();
         }
@@ -476,17 +480,15 @@ private:
         }
     }
 
-    // Completion: lanes finish in launch order.
-    void complete()
+    // Completion of one lane's batches (each lane has its own thread).
+    void complete(Lane& lane)
     {
+        Lane* L = &lane;
         for (;;) {
-            Lane* L = nullptr;
             {
                 std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait(lk, [&] { return !pending_.empty() || (stop_ && queue_.empty() && inflight_ == 0); });
-                if (pending_.empty()) return;
-                L = pending_.front();
-                pending_.pop_front();
+                cv_.wait(lk, [&] { return L->launched || (stop_ && queue_.empty() && !L->busy); });
+                if (!L->launched) return;
             }
             const cudaError_t e = cudaEventSynchronize(L->done);
             std::string err = L->error;
@@ -522,6 +524,7 @@ private:
                 }
                 inflight_ -= (int)L->reqs.size();
                 L->reqs.clear();
+                L->launched = false;
                 L->busy = false;
             }
             done_cv_.notify_all();
@@ -537,7 +540,7 @@ private:
     std::mutex mu_;
     std::condition_variable cv_, done_cv_;
     std::deque<Request*> queue_;
-    std::deque<Lane*> pending_;
+
     std::unordered_map<long long, std::unique_ptr<Request>> all_;
     long long next_id_ = 0;
     int inflight_ = 0;
@@ -546,7 +549,8 @@ private:
     std::vector<double> lat_ms_;
     long long ok_ = 0, failed_ = 0, refused_ = 0, batches_ = 0, batched_pairs_ = 0, max_inflight_pairs_ = 0;
     double first_submit_ = 0, last_done_ = 0;
-    std::thread sched_, comp_;
+    std::thread sched_;
+    std::vector<std::thread> comps_;
 };
 
 }  // namespace pg
