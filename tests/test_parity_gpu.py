@@ -134,3 +134,49 @@ def test_packed_shapes_odd_widths_match_reference(case, words):
         other = _runners.run_oracle(case, _runners.device_lut(case))
     bad = _runners.compare(mine, other)
     assert not bad, bad
+
+
+def test_full_size_batched_pairs_match_reference_kernels():
+    """The benchmark workload at full size -- 1920x1080, D=256,
+    pyramid_levels=3, adaptive P2, 3x3 median, all three outputs -- for two
+    Census and two BT pairs run together through the batch engine (so the
+    level launches take the many-row kernel shapes), against the
+    reference's kernels on its StereoMatcher schedule, pair by pair."""
+    import torch
+    import pyrsgm_gb300 as pg
+    from pyrsgm_gb300 import synth
+    if not _oracle.ref_available():
+        pytest.skip("reference kernels not built (oracle/_ref)")
+    w, h = 1920, 1080
+
+    def params(cost):
+        return dict(num_disparities=256, pyramid_levels=3, cost_mode=cost,
+                    p1=8 if cost == cases.CENSUS else 300, p2=32 if cost == cases.CENSUS else 2400,
+                    adaptive_p2=True, median_filter=True, lr_check=True, uniqueness_ratio=10,
+                    pyramid_coarse_disparities=128)
+
+    costs = [cases.CENSUS, cases.BT, cases.CENSUS, cases.BT]
+    pairs = [synth.make_pair(w, h, 255, 16, 3000 + i)[:2] for i in range(len(costs))]
+    items, outs = [], []
+    for (left, right), c in zip(pairs, costs):
+        o = dict(disp16=torch.zeros((h, w), dtype=torch.int16, device="cuda"),
+                 disp32=torch.zeros((h, w), dtype=torch.float32, device="cuda"),
+                 conf=torch.zeros((h, w), dtype=torch.float32, device="cuda"))
+        items.append(dict(left=torch.from_numpy(left).cuda(), right=torch.from_numpy(right).cuda(),
+                          params=pg.Params(**params(c)), **o))
+        outs.append(o)
+    eng = pg.BatchEngine(16 << 30)
+    st = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    eng.run(items, use_graph=True, stream=st)
+    torch.cuda.synchronize()
+    for i, ((left, right), c) in enumerate(zip(pairs, costs)):
+        r16 = torch.zeros((h, w), dtype=torch.int16, device="cuda")
+        r32 = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+        rcf = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+        _runners._ref_matcher(dict(w=w, h=h, params=params(c)), items[i]["left"], items[i]["right"], r16, r32, rcf)
+        np.testing.assert_array_equal(outs[i]["disp16"].cpu().numpy(), r16.cpu().numpy(), err_msg=f"pair {i}")
+        np.testing.assert_allclose(outs[i]["disp32"].cpu().numpy(), r32.cpu().numpy(), rtol=0, atol=1e-6)
+        np.testing.assert_allclose(outs[i]["conf"].cpu().numpy(), rcf.cpu().numpy(), rtol=0, atol=1e-6)
+        assert int((outs[i]["disp16"] > 0).sum()) > w * h // 2
+    eng.close()
