@@ -325,6 +325,10 @@ __device__ __forceinline__ void wta_out(const LevelDesc& J, int y, int x, int ba
 // bandwidth of line requests.  SC chunk slots in flight per warp.
 template <int D>
 __host__ __device__ constexpr int chunk_steps() { return D >= 64 ? 1 : 64 / D; }
+// Chunk slots per warp (SC - 1 runs in flight): for 4-step runs 3 measured
+// fastest on the 16-pair 1080p row pass (2: too little look-ahead; 4: the
+// larger footprint was slower as well); shorter runs keep about 6-8 steps
+// of look-ahead.
 template <int D>
 __host__ __device__ constexpr int chunk_stages() { return chunk_steps<D>() == 4 ? 3 : chunk_steps<D>() == 2 ? 4 : 6; }
 
