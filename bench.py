@@ -481,9 +481,7 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
     clk.__exit__(None, None, None)
     e2e_total = sum(e2e_ms)
     if world > 1:
-        t = torch.tensor([total_ms, e2e_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_total = float(t[0].item()), float(t[1].item())
+        total_ms, e2e_total = replica_max(dist, [total_ms, e2e_total], dev)
     return dict(total_ms=total_ms, step_ms=step_ms, pair_ms=pair_ms, launches=launches, prof=prof,
                 prof_steps=1 if graph else args.steps,
                 clocks=clk.summary(), e2e_total=e2e_total, e2e_steps=len(e2e_ms),
@@ -609,6 +607,20 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
             "server": served, "plain_sequential": plain}
 
 
+def replica_max(dist, values, device) -> list:
+    """Each timing's maximum over the ranks: the slowest replica bounds the
+    job (replicas exchange nothing else)."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def job_rate(world: int, units_per_rank: float, max_ms: float) -> float:
+    """Whole-job throughput: the units of every rank over the slowest rank's time."""
+    return world * units_per_rank / (max_ms / 1e3)
+
+
 def _pct(v, q):
     s = sorted(v)
     return s[max(0, min(len(s) - 1, int(round(q * (len(s) - 1)))))]
@@ -648,8 +660,8 @@ def run(args) -> dict | None:
             measure(BatchRunner(pairs, dev), args, stream, flush, dev, world, dist, True, False)
         if args.mode == "plain":
             headline = measure(MineRunner(pairs, dev), args, stream, flush, dev, world, dist, True, True)
-    value = world * npairs / (headline["total_ms"] / 1e3)
-    e2e_value = world * args.batch * headline["e2e_steps"] / (headline["e2e_total"] / 1e3)
+    value = job_rate(world, npairs, headline["total_ms"])
+    e2e_value = job_rate(world, args.batch * headline["e2e_steps"], headline["e2e_total"])
     if rank != 0:
         return None
     out = {
