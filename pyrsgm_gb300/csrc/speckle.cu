@@ -9,9 +9,10 @@
 // larger index -> smaller with atomicCAS): first inside each 32x8 tile in
 // shared memory, each pixel linking its right and lower neighbour, which
 // leaves every pixel pointing at its tile-local root; then across tile
-// borders in global memory; then root sizes by atomicAdd and one pass that
-// clears small regions.  The partition into regions is unique, so the
-// output is exactly that of a sequential flood fill.
+// borders in global memory; then root sizes (atomicAdd, one per distinct
+// root and warp) and one pass that clears small regions.  The partition into
+// regions is unique, so the output is exactly that of a sequential flood
+// fill.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -120,15 +121,22 @@ __global__ void k_sp_link(const SpArgs A)
     }
 }
 
-__global__ void k_sp_count(const SpArgs A)
+__global__ void __launch_bounds__(256) k_sp_count(const SpArgs A)
 {
-    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x >= A.w || y >= A.h) return;
-    const int p = y * A.w + x;
-    if (A.lab[p] < 0) return;
-    const int r = sp_find(A.lab, p);
-    A.lab[p] = r;
-    atomicAdd(&A.size[r], 1);
+    const int lane = threadIdx.x & 31;
+    const int x = blockIdx.x * 32 + lane, y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    int r = -1 - lane;   // outside the image or new_val: a key no other lane has
+    if (x < A.w && y < A.h) {
+        const int p = y * A.w + x;
+        if (A.lab[p] >= 0) {
+            r = sp_find(A.lab, p);
+            A.lab[p] = r;
+        }
+    }
+    // one atomic per distinct root in the warp (a large region's pixels
+    // would otherwise queue on a single counter); all 32 lanes take part
+    const unsigned peers = __match_any_sync(0xffffffffu, r);
+    if (r >= 0 && lane == __ffs(peers) - 1) atomicAdd(&A.size[r], __popc(peers));
 }
 
 __global__ void k_sp_apply(const SpArgs A)
@@ -136,8 +144,11 @@ __global__ void k_sp_apply(const SpArgs A)
     const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= A.w || y >= A.h) return;
     const int p = y * A.w + x;
-    const int r = A.lab[p];
-    if (r >= 0 && A.size[r] <= A.max_size) A.d[(size_t)y * A.pitch + x] = (short)A.new_val;
+    if (A.lab[p] < 0) return;
+    // the root again: path halving by other threads of the count pass may
+    // have pointed lab[p] at an ancestor after its own thread stored the root
+    const int r = sp_find(A.lab, p);
+    if (A.size[r] <= A.max_size) A.d[(size_t)y * A.pitch + x] = (short)A.new_val;
 }
 
 }  // namespace
