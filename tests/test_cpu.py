@@ -213,3 +213,36 @@ def test_autotune_switch_and_empty_table_without_device_work():
         assert pg.autotune_table() == []
     finally:
         pg.set_autotune(prev)
+
+
+def test_new_entry_points_reject_bad_arguments_without_device_work():
+    """Speckle filter, plan reservation and the autotune table check their
+    arguments before any device call."""
+    lib = _native.lib()
+    # filter_speckles: null map, empty size, odd or short pitch, negative max_diff
+    assert lib.pyrsgm_gb300_filter_speckles(None, 64, 32, 8, -16, 10, 1, None) == -1
+    assert lib.pyrsgm_gb300_filter_speckles(1, 64, 0, 8, -16, 10, 1, None) == -1
+    assert lib.pyrsgm_gb300_filter_speckles(1, 63, 31, 8, -16, 10, 1, None) == -1
+    assert lib.pyrsgm_gb300_filter_speckles(1, 32, 32, 8, -16, 10, 1, None) == -1
+    assert lib.pyrsgm_gb300_filter_speckles(1, 64, 32, 8, -16, 10, -1, None) == -1
+    assert lib.pyrsgm_gb300_filter_speckles(1, 64, 32, 8, -16, 0, 1, None) == 0   # max size 0: nothing to do
+    # batch reservation: null engine / params, empty size, invalid parameters
+    import pyrsgm_gb300 as pg
+    p = pg.Params(num_disparities=64, pyramid_levels=1)
+    err = C.create_string_buffer(256)
+    eng = lib.pyrsgm_gb300_batch_create(1 << 20, err, 256)
+    assert eng
+    try:
+        assert lib.pyrsgm_gb300_batch_reserve(None, 64, 48, C.byref(p.to_c()), 1, None, err, 256) == -1
+        assert lib.pyrsgm_gb300_batch_reserve(eng, 64, 48, None, 1, None, err, 256) == -1
+        assert lib.pyrsgm_gb300_batch_reserve(eng, 0, 48, C.byref(p.to_c()), 1, None, err, 256) == -1
+        bad = pg.Params(num_disparities=64, pyramid_levels=9)   # validateParams rejects it
+        assert lib.pyrsgm_gb300_batch_reserve(eng, 64, 48, C.byref(bad.to_c()), 1, None, err, 256) == -1
+        assert b"pyramid_levels" in err.value
+        assert lib.pyrsgm_gb300_batch_bytes_in_use(eng) == 0
+    finally:
+        lib.pyrsgm_gb300_batch_destroy(eng)
+    assert lib.pyrsgm_gb300_server_reserve(None, 64, 48, C.byref(p.to_c()), 1, err, 256) == -1
+    # the autotune table can be sized with a null buffer
+    pg.autotune_clear()
+    assert lib.pyrsgm_gb300_autotune_entries(None, 0) == 0
