@@ -621,6 +621,17 @@ def job_rate(world: int, units_per_rank: float, max_ms: float) -> float:
     return world * units_per_rank / (max_ms / 1e3)
 
 
+def stage_bandwidth(prof: dict, peak_gbs: float) -> dict:
+    """Algorithmic bytes over measured time for each profiled stage, in GB/s
+    and as a fraction of the HBM peak (the issue-bound stages stay low)."""
+    out = {}
+    for k, v in prof.items():
+        if v.get("launches") and v.get("ms", 0) > 0 and v.get("bytes", 0) > 0:
+            gbs = v["bytes"] / (v["ms"] / 1e3) / 1e9
+            out[k] = {"gbs": round(gbs, 1), "frac": round(gbs / peak_gbs, 4)}
+    return out
+
+
 def _pct(v, q):
     s = sorted(v)
     return s[max(0, min(len(s) - 1, int(round(q * (len(s) - 1)))))]
@@ -700,6 +711,7 @@ def run(args) -> dict | None:
                            "avg_launch_ms": round(row["ms"] / row["launches"], 5) if row.get("launches") else None}
         out["kernels_ms_per_step"] = {k: round(v["ms"] / headline["prof_steps"], 4)
                                       for k, v in prof.items() if v["launches"]}
+        out["kernels_hbm"] = stage_bandwidth(prof, pk["hbm_gbs"])
         if args.mode == "batched":
             import pyrsgm_gb300 as pg
             out["autotune"] = pg.autotune_table()

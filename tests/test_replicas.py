@@ -50,3 +50,12 @@ def test_job_rate_counts_every_rank_over_the_slowest_time():
     # two replicas, 320 pairs each, the slower one taking 160 ms
     assert bench.job_rate(2, 320, 160.0) == pytest.approx(4000.0)
     assert bench.job_rate(1, 320, 160.0) == pytest.approx(2000.0)
+
+
+def test_stage_bandwidth_from_profiler_records():
+    import bench
+    prof = {"path_row": {"ms": 2.0, "launches": 4, "bytes": 8e9},
+            "cost": {"ms": 4.0, "launches": 3, "bytes": 1e9},
+            "p2table": {"ms": 0.0, "launches": 0, "bytes": 0.0}}
+    got = bench.stage_bandwidth(prof, 8000.0)
+    assert got == {"path_row": {"gbs": 4000.0, "frac": 0.5}, "cost": {"gbs": 250.0, "frac": 0.0312}}
