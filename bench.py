@@ -692,6 +692,10 @@ def run(args) -> dict | None:
                 **({"trials_ms_per_step": headline["e2e_trials"]} if headline.get("e2e_trials") else {})},
         "gpu_launches": headline["launches"],
         "clocks": headline["clocks"],
+        # the same rates per full-resolution pixel and per pixel-disparity
+        "throughput": {"mpix_per_s": round(value * W * H / 1e6, 1),
+                       "mpix_d_per_s": round(value * W * H * D / 1e6, 1),
+                       "e2e_mpix_per_s": round(e2e_value * W * H / 1e6, 1)},
     }
     if plain["pair_ms"]:
         out["plain_compute"] = {"value": round(world * npairs / (plain["total_ms"] / 1e3), 3), "unit": "pairs/s",
