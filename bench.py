@@ -637,44 +637,11 @@ def _pct(v, q):
     return s[max(0, min(len(s) - 1, int(round(q * (len(s) - 1)))))]
 
 
-def run(args) -> dict | None:
-    import torch
-    import torch.distributed as dist
-
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl" if args.impl == "mine" else "gloo")
-    if args.impl == "reference" and rank != 0:
-        return None
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    if args.impl == "reference":
-        from tests import _oracle
-        if not _oracle.ref_available():
-            print(json.dumps({"impl": "reference", "unavailable": "reference kernels (oracle/_ref) not built"}))
-            return None
-
-    pairs = make_inputs(args.batch)
-    stream = torch.cuda.Stream(device=dev)
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
-    pk = peaks()
-    npairs = args.batch * args.steps
-
-    if args.impl == "reference":
-        m = measure(ReferenceRunner(pairs, dev), args, stream, flush, dev, 1, dist, False, True)
-        headline, plain = m, m
-    else:
-        plain = measure(MineRunner(pairs, dev), args, stream, flush, dev, world, dist, False, True)
-        headline = plain if args.mode == "plain" else \
-            measure(BatchRunner(pairs, dev), args, stream, flush, dev, world, dist, True, False)
-        if args.mode == "plain":
-            headline = measure(MineRunner(pairs, dev), args, stream, flush, dev, world, dist, True, True)
+def result_line(args, world: int, headline: dict, plain: dict, pk: dict, npairs: int) -> dict:
+    """The JSON line of a run from its measurements (`measure()` records of
+    the headline and the plain per-pair runs, the HBM peak)."""
     value = job_rate(world, npairs, headline["total_ms"])
     e2e_value = job_rate(world, args.batch * headline["e2e_steps"], headline["e2e_total"])
-    if rank != 0:
-        return None
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(headline["total_ms"] / args.steps, 4),
@@ -716,13 +683,54 @@ def run(args) -> dict | None:
         out["kernels_ms_per_step"] = {k: round(v["ms"] / headline["prof_steps"], 4)
                                       for k, v in prof.items() if v["launches"]}
         out["kernels_hbm"] = stage_bandwidth(prof, pk["hbm_gbs"])
-        if args.mode == "batched":
-            import pyrsgm_gb300 as pg
-            out["autotune"] = pg.autotune_table()
-            pg.set_autotune(False)
     else:
         out["impl"] = "reference"
         out["reference_build"] = "reference src/sgm_kernels.cu + src/pyrdown.cu compiled unmodified for sm_103a"
+    return out
+
+
+def run(args) -> dict | None:
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if args.impl == "mine" else "gloo")
+    if args.impl == "reference" and rank != 0:
+        return None
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if args.impl == "reference":
+        from tests import _oracle
+        if not _oracle.ref_available():
+            print(json.dumps({"impl": "reference", "unavailable": "reference kernels (oracle/_ref) not built"}))
+            return None
+
+    pairs = make_inputs(args.batch)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    pk = peaks()
+    npairs = args.batch * args.steps
+
+    if args.impl == "reference":
+        m = measure(ReferenceRunner(pairs, dev), args, stream, flush, dev, 1, dist, False, True)
+        headline, plain = m, m
+    else:
+        plain = measure(MineRunner(pairs, dev), args, stream, flush, dev, world, dist, False, True)
+        headline = plain if args.mode == "plain" else \
+            measure(BatchRunner(pairs, dev), args, stream, flush, dev, world, dist, True, False)
+        if args.mode == "plain":
+            headline = measure(MineRunner(pairs, dev), args, stream, flush, dev, world, dist, True, True)
+    if rank != 0:
+        return None
+    out = result_line(args, world, headline, plain, pk, npairs)
+    value = out["value"]
+    if args.impl == "mine" and args.mode == "batched":
+        import pyrsgm_gb300 as pg
+        out["autotune"] = pg.autotune_table()
+        pg.set_autotune(False)
     if args.impl == "mine" and world == 1:
         out["latency_1080p_d256_l2_census"] = single_pair_latency(dev, stream)
     if args.impl == "mine" and world == 1 and args.serve_requests > 0:

@@ -1,8 +1,9 @@
-"""Several GPUs run independent replicas (pairs are independent units; no
-data is exchanged).  The only cross-rank step is the benchmark's timing
-reduction: each timing's maximum over the ranks, and the job's rate = all
-ranks' pairs over the slowest rank's time.  Checked here with two gloo
-ranks on the CPU."""
+"""Host-side logic of the benchmark.  Several GPUs run independent
+replicas (pairs are independent units; no data is exchanged): the only
+cross-rank step is the timing reduction -- each timing's maximum over the
+ranks, and the job's rate = all ranks' pairs over the slowest rank's time
+-- checked here with two gloo ranks on the CPU.  The JSON line is assembled
+from measurement records by a pure function, checked on made-up records."""
 from __future__ import annotations
 
 import os
@@ -59,3 +60,36 @@ def test_stage_bandwidth_from_profiler_records():
             "p2table": {"ms": 0.0, "launches": 0, "bytes": 0.0}}
     got = bench.stage_bandwidth(prof, 8000.0)
     assert got == {"path_row": {"gbs": 4000.0, "frac": 0.5}, "cost": {"gbs": 250.0, "frac": 0.0312}}
+
+
+def _record(total_ms, prof=None, trials=None):
+    """A record shaped like bench.measure()'s."""
+    return dict(total_ms=total_ms, step_ms=[total_ms / 10] * 10, pair_ms=[1.3, 1.31, 1.32], launches=370,
+                prof=prof or {}, prof_steps=1,
+                clocks={"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": [], "samples": 20},
+                e2e_total=8 * 13.7, e2e_steps=8, e2e_trials=trials)
+
+
+def test_result_line_keeps_the_contract_keys():
+    import argparse
+    import bench
+    args = argparse.Namespace(batch=32, steps=10, warmup=3, mode="batched", impl="mine")
+    prof = {"path_row": {"ms": 2.8, "launches": 4, "bytes": 11.9e9},
+            "cost": {"ms": 4.36, "launches": 3, "bytes": 1.6e9},
+            "p2table": {"ms": 0.0, "launches": 0, "bytes": 0.0}}
+    head = _record(132.7, prof, [13.7, 13.7, 19.6, 13.7, 13.7])
+    out = bench.result_line(args, 1, head, _record(384.0), {"hbm_gbs": 6795.1, "source": "measured"}, 320)
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "e2e", "gpu_launches", "clocks", "roofline", "throughput"):
+        assert k in out, k
+    assert out["value"] == round(320 / 0.1327, 3)
+    assert out["e2e"]["value"] == round(32 * 8 / (8 * 13.7 / 1e3), 3)
+    assert set(out["e2e"]) >= {"value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"}
+    assert out["roofline"]["bound"] == "hbm" and 0 < out["roofline"]["frac"] < 1
+    assert set(out["roofline"]) >= {"achieved", "peak", "unit", "frac", "traffic"}
+    assert out["throughput"]["mpix_per_s"] == round(out["value"] * 1920 * 1080 / 1e6, 1)
+    assert set(out["kernels_hbm"]) == {"path_row", "cost"}
+    assert out["kernels_ms_per_step"]["path_row"] == 2.8
+    ref = bench.result_line(argparse.Namespace(batch=32, steps=10, warmup=3, mode="batched", impl="reference"), 1,
+                            _record(4146.6), _record(4146.6), {"hbm_gbs": 6795.1, "source": "measured"}, 320)
+    assert ref["impl"] == "reference" and "roofline" not in ref
