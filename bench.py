@@ -725,7 +725,8 @@ def run(args) -> dict | None:
             headline = measure(MineRunner(pairs, dev), args, stream, flush, dev, world, dist, True, True)
     if rank != 0:
         return None
-    out = result_line(args, world, headline, plain, pk, npairs)
+    # the reference arm runs on rank 0 alone
+    out = result_line(args, 1 if args.impl == "reference" else world, headline, plain, pk, npairs)
     value = out["value"]
     if args.impl == "mine" and args.mode == "batched":
         import pyrsgm_gb300 as pg
