@@ -42,8 +42,10 @@ size_t pyrsgm_gb300_workspace_bytes(int width, int height, int numDisparities);
  * (pyrsgm_gb300_workspace_bytes(width, height, numDisparities) <= 32 MiB,
  * e.g. 480x360 at 16 labels) or the call returns -1.  The first call on a
  * device looks up the array's device address (make it before any stream
- * capture).  All calls share the array: calls whose GPU work overlaps race
- * and must be serialised by the caller. */
+ * capture) and keeps it for the life of the process: do not call it from a
+ * context other than the device's primary context, nor after
+ * cudaDeviceReset.  All calls share the array: calls whose GPU work
+ * overlaps race and must be serialised by the caller. */
 int pyrsgm_gb300_compute_level_noalloc(
     const unsigned char* d_left_gray, const unsigned char* d_right_gray,
     const short* d_parent_disp, const float* d_parent_conf,
@@ -212,6 +214,21 @@ int pyrsgm_gb300_filter_speckles(short* d_disp, size_t pitch_bytes, int width, i
  * setting, or -1 for another value.  The environment variable
  * PYRSGM_GB300_PACKED_NW gives the initial setting. */
 int pyrsgm_gb300_set_packed_words(int words);
+
+/* Fused aggregation of the 16-label pyramid levels with three paths (on by
+ * default; PYRSGM_GB300_FUSED=0 turns it off at load).  When on, the wide
+ * shape of those levels is two passes -- top-to-bottom and left-to-right
+ * together on a skewed front of 32-row bands (each band waits, bounded, for
+ * the band above's bottom edge), then right-to-left with the
+ * winner-take-all -- instead of three path passes and a winner-take-all
+ * pass; results are identical.  Returns the previous setting. */
+int pyrsgm_gb300_set_fused(int on);
+
+/* Waits of the fused pass that ran out of time (a band whose band above
+ * never published its edge; results of that launch are wrong), counted on
+ * the current device since load or the last reset.  Synchronous.
+ * 0xffffffff if the count could not be read. */
+unsigned pyrsgm_gb300_fused_stalls(int reset);
 
 /* Measuring choice of that shape (off by default; the environment variable
  * PYRSGM_GB300_AUTOTUNE=1 turns it on at load).  When on, the first run of

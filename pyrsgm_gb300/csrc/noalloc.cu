@@ -23,7 +23,10 @@
 // host it is only a shadow symbol).  The first call on a device, with that
 // device current, asks the runtime for the address once
 // (cudaGetSymbolAddress) and caches it per device; make that first call
-// before any stream capture.
+// before any stream capture.  The cached address belongs to the device's
+// primary context: a call from another context on that device, or after
+// cudaDeviceReset (which reloads the module, possibly elsewhere), would use
+// a stale address, so neither is supported.
 //
 // Sharing.  All calls on a device use the same array and it keeps the last
 // call's contents.  Nothing in it has to start at zero: every region a call

@@ -31,6 +31,9 @@ def acc_cols(case: dict) -> tuple[int, int]:
 
 
 def inputs(case: dict):
+    if "pair" in case:   # explicit images (the full-size configuration cases)
+        left, right = case["pair"]
+        return left, right, (None, None)
     left, right, truth = pair_for(case)
     parent = parent_for(case, truth) if case["kind"] == "level" and case["refine"] else (None, None)
     return left, right, parent
@@ -233,6 +236,97 @@ def run_ref(case: dict) -> dict:
         ref.ref_destroy_workspace(ws)
     out.update(disp16=d16.cpu().numpy(), disp32=d32.cpu().numpy(), conf=cf.cpu().numpy(), acc_cols=acc_cols(case))
     return out
+
+
+def matcher_levels(w: int, h: int, params: dict, left: np.ndarray, right: np.ndarray) -> list[dict]:
+    """The StereoMatcher::compute schedule (reference src/stereo_matcher.cpp:238-338)
+    run level by level through the C API, once on this library and once on the
+    reference kernels, each feeding its own coarser output to the next level.
+    Returns one record per level (coarsest first) with both sides' outputs and
+    volumes (cost and aggregated, as run_mine / run_ref give them), the
+    pyramid images of both, and the level geometry."""
+    torch = _torch()
+    import pyrsgm_gb300 as pg
+    ref = _oracle.ref()
+    v = _oracle.orc_validate(**params)
+    info = _oracle.orc_geometry(w, h, **params)
+    levels = v["pyramid_levels"]
+    assert levels >= 1
+    st = torch.cuda.current_stream().cuda_stream
+    p2a = (v["p2_alpha"], v["p2_beta"], v["p2_lower_mult"], v["p2_upper_mult"])
+
+    def post(level):
+        if level != 0:
+            return 1
+        return (1 if v["lr_check"] else 0) | (2 if v["median_filter"] else 0)
+
+    img = {"mine": {0: (_dev(left), _dev(right))}, "ref": {0: (_dev(left), _dev(right))}}
+    for l in range(1, levels + 1):
+        li, par = info[l], info[l - 1]
+        for side in ("mine", "ref"):
+            pair = []
+            for src in img[side][l - 1]:
+                dst = torch.zeros((li["height"], li["width"]), dtype=torch.uint8, device="cuda")
+                if side == "mine":
+                    pg.pyrdown(src, dst)
+                else:
+                    assert ref.ref_pyrdown_u8(src.data_ptr(), par["width"], par["width"], par["height"],
+                                              dst.data_ptr(), li["width"], li["width"], li["height"], st) == 0
+                pair.append(dst)
+            img[side][l] = tuple(pair)
+    outs = {"mine": {}, "ref": {}}
+    records = []
+    for l in range(levels, -1, -1):
+        li = info[l]
+        lw, lh, D = li["width"], li["height"], li["num_labels"]
+        refine = bool(li["refine"])
+        rec = {"level": l, "w": lw, "h": lh, "D": D, "refine": refine}
+        for side in ("mine", "ref"):
+            d16 = torch.zeros((lh, lw), dtype=torch.int16, device="cuda")
+            d32 = torch.zeros((lh, lw), dtype=torch.float32, device="cuda") if l == 0 else None
+            cf = torch.zeros((lh, lw), dtype=torch.float32, device="cuda")
+            par = outs[side].get(l + 1)
+            pw = info[l + 1]["width"] if refine else 0
+            ph = info[l + 1]["height"] if refine else 0
+            L, R = img[side][l]
+            kw = dict(num_disparities=D, min_disparity=v["min_disparity"], max_disparity=li["max_disparity"],
+                      block_size=li["block_size"], p1=v["p1"], p2=v["p2"], uniqueness=v["uniqueness_ratio"],
+                      disp12_max_diff=v["disp12_max_diff"], pre_filter_cap=v["pre_filter_cap"],
+                      cost_mode=v["cost_mode"], post_flags=post(l), num_paths=v["num_paths"], refine=refine,
+                      min_confidence=v["pyramid_min_confidence"], adaptive_p2=bool(v["adaptive_p2"]),
+                      p2_alpha=p2a[0], p2_beta=p2a[1], p2_lower=p2a[2], p2_upper=p2a[3])
+            if side == "mine":
+                ws = pg.Workspace()
+                ws.set_debug(1)
+                assert pg.compute_level(ws, L, R, par[0] if refine else None, par[1] if refine else None,
+                                        d16, d32, cf, **kw) == 0
+                cost, acc = ws.volumes()
+                torch.cuda.synchronize()
+                ws.close()
+            else:
+                ws = ref.ref_create_workspace()
+                r = ref.ref_compute_level(ws, L.data_ptr(), R.data_ptr(),
+                                          par[0].data_ptr() if refine else None,
+                                          par[1].data_ptr() if refine else None,
+                                          d16.data_ptr(), d32.data_ptr() if d32 is not None else None, cf.data_ptr(),
+                                          lw, lw, pw * 2, pw * 4, lw * 2, lw * 4, lw * 4, lw, lh, pw, ph, D,
+                                          v["min_disparity"], li["max_disparity"], li["block_size"], v["p1"],
+                                          v["p2"], v["uniqueness_ratio"], v["disp12_max_diff"],
+                                          v["pre_filter_cap"], v["cost_mode"], post(l), v["num_paths"],
+                                          1 if refine else 0, v["pyramid_min_confidence"], v["adaptive_p2"], *p2a,
+                                          st)
+                assert r == 0, ref.ref_last_error()
+                cost = torch.empty((lh, lw, D), dtype=torch.int16, device="cuda")
+                acc = torch.empty_like(cost)
+                assert ref.ref_copy_volumes(ws, cost.data_ptr(), acc.data_ptr(), st) == 0
+                torch.cuda.synchronize()
+                ref.ref_destroy_workspace(ws)
+            outs[side][l] = (d16, cf)
+            rec[side] = dict(disp16=d16.cpu().numpy(), disp32=d32.cpu().numpy() if d32 is not None else None,
+                             conf=cf.cpu().numpy(), cost=cost.cpu().numpy(), acc=acc.cpu().numpy(),
+                             acc_cols=(0, lw), left=L.cpu().numpy(), right=R.cpu().numpy())
+        records.append(rec)
+    return records
 
 
 def run_ref_pyrdown(src: np.ndarray) -> np.ndarray:
