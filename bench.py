@@ -14,10 +14,11 @@ reference's headline metric is quoted on).
           copies the three outputs device->host; two slots let one step's
           copies overlap its neighbours' compute, and the events span all
           steps, copies included
-  roofline  the dominant kernel (the row pass: L->R + R->L sums of the 16/32
-          label levels) timed with CUDA events on its stream via the library
-          profiler, its algorithmic bytes / duration against the measured
-          HBM peak
+  roofline  the aggregation kernels of one step, each timed with CUDA events
+          on its stream via the library profiler: the algorithmic bytes of
+          the aggregation (4 B per voxel: the partial aggregated volume
+          written and read once) over their summed duration, against the
+          measured HBM peak; pipeline_roofline the same for the whole step
 
 --impl reference runs the reference's own CUDA kernels (compiled from its
 sources into oracle/_ref/ and launched by oracle/_build/libref_harness.so)
@@ -52,10 +53,28 @@ def params_for(cost: int) -> dict:
                 pyramid_coarse_disparities=128)
 
 
-# DRAM bytes per algorithmic byte of k_grow, from one ncu capture of its
-# level-0 launch for eight 1080p pairs (dram read + write 2.147 GB against
-# 2.223 GB algorithmic; part of the second read of the cost volume hits L2).
-K_GROW_TRAFFIC_PER_ALG_BYTE = 0.966
+# Measured DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of
+# the aggregation launches per algorithmic byte, filled in from the committed
+# capture of the aggregation kernels (None: no capture of this build yet).
+AGG_TRAFFIC_PER_ALG_BYTE = None
+
+
+def alg_bytes(width: int, height: int, params: dict) -> dict:
+    """Algorithmic device-memory bytes of one pair: every level's partial
+    aggregated volume written and read once as int16 (4 B per voxel; costs
+    recomputed on chip), both u8 views read, the outputs (disp16 + disp32 +
+    conf at level 0; disparity and confidence written and read by the child
+    on the other levels) and the pyramid (parent views read, child views
+    written).  'aggregation' is the volume term alone."""
+    import pyrsgm_gb300 as pg
+    info = pg.level_geometry(width, height, pg.Params(**params))
+    agg = sum(4.0 * li.width * li.height * li.num_labels for li in info)
+    px = [li.width * li.height for li in info]
+    views = sum(2.0 * p for p in px)
+    outs = 10.0 * px[0] + sum(12.0 * p for p in px[1:])
+    pyr = sum(2.0 * px[l - 1] + 2.0 * px[l] for l in range(1, len(px)))
+    return {"aggregation": agg, "total": agg + views + outs + pyr,
+            "voxels": sum(float(li.width * li.height * li.num_labels) for li in info)}
 
 
 def peaks() -> dict:
@@ -435,8 +454,7 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
             runner.step_direct(stream)
         torch.cuda.synchronize()
     if lib is not None:
-        names = ["pyrdown", "features", "labels", "cost", "path_tb", "path_row", "post", "p2table", "wta"]
-        for k, nm in enumerate(names):
+        for k, nm in enumerate(PROF_NAMES):
             ms, cnt, by = C.c_double(), C.c_longlong(), C.c_double()
             lib.pyrsgm_gb300_profile_read(k, C.byref(ms), C.byref(cnt), C.byref(by))
             prof[nm] = {"ms": ms.value, "launches": cnt.value, "bytes": by.value}
@@ -621,6 +639,14 @@ def job_rate(world: int, units_per_rank: float, max_ms: float) -> float:
     return world * units_per_rank / (max_ms / 1e3)
 
 
+# profiled stages of the aggregation and the kernels behind them
+AGG_STAGES = ("path_tb", "path_row", "wta", "tblr", "rlw")
+AGG_KERNELS = {"path_tb": "k_gtb/k_path_tb", "path_row": "k_grow/k_path_row", "wta": "k_wta",
+               "tblr": "k_tblr", "rlw": "k_rlw"}
+PROF_NAMES = ["pyrdown", "features", "labels", "cost", "path_tb", "path_row", "post", "p2table", "wta", "tblr",
+              "rlw"]
+
+
 def stage_bandwidth(prof: dict, peak_gbs: float) -> dict:
     """Algorithmic bytes over measured time for each profiled stage, in GB/s
     and as a fraction of the HBM peak (the issue-bound stages stay low)."""
@@ -670,18 +696,34 @@ def result_line(args, world: int, headline: dict, plain: dict, pk: dict, npairs:
                                 "latency_ms_p99": round(_pct(plain["pair_ms"], 0.99), 4)}
     if args.impl == "mine":
         prof = headline["prof"]
-        row = prof.get("path_row", {})
-        achieved = (row["bytes"] / (row["ms"] / 1e3) / 1e9) if row.get("ms") else None
-        out["roofline"] = {"kernel": "k_grow (L->R and R->L path costs of the 16/32-label levels)", "bound": "hbm",
-                           "achieved": round(achieved, 2) if achieved else None, "peak": pk["hbm_gbs"],
-                           "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4) if achieved else None,
-                           "peak_source": pk["source"],
-                           "traffic": round(K_GROW_TRAFFIC_PER_ALG_BYTE * row["bytes"] / row["launches"] / 1e9, 4)
-                           if row.get("launches") else None,
-                           "traffic_unit": "GB per launch (ncu capture scaled by voxels)",
-                           "avg_launch_ms": round(row["ms"] / row["launches"], 5) if row.get("launches") else None}
-        out["kernels_ms_per_step"] = {k: round(v["ms"] / headline["prof_steps"], 4)
-                                      for k, v in prof.items() if v["launches"]}
+        ps = headline["prof_steps"]
+        per_pair = {c: alg_bytes(W, H, params_for(c)) for c in (CENSUS, BT)}
+        step_pairs = [CENSUS if i % 2 == 0 else BT for i in range(args.batch)]
+        agg_alg = sum(per_pair[c]["aggregation"] for c in step_pairs)     # bytes per step
+        tot_alg = sum(per_pair[c]["total"] for c in step_pairs)
+        agg_keys = [k for k in AGG_STAGES if prof.get(k, {}).get("launches")]
+        agg_ms = sum(prof[k]["ms"] for k in agg_keys) / ps
+        agg_launches = sum(prof[k]["launches"] for k in agg_keys) / ps
+        own = sum(prof[k]["bytes"] for k in agg_keys) / ps
+        achieved = agg_alg / (agg_ms / 1e3) / 1e9 if agg_ms > 0 else None
+        out["roofline"] = {
+            "kernel": "aggregation (" + " + ".join(AGG_KERNELS[k] for k in agg_keys) + "), one step",
+            "bound": "hbm",
+            "achieved": round(achieved, 2) if achieved else None, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / pk["hbm_gbs"], 4) if achieved else None, "peak_source": pk["source"],
+            "algorithmic": "4 B per voxel (partial aggregated volume written and read once as int16)",
+            "alg_bytes_per_step": round(agg_alg / 1e9, 4),
+            "implementation_bytes_per_step": round(own / 1e9, 4),
+            "traffic": round(AGG_TRAFFIC_PER_ALG_BYTE * own / 1e9, 4) if AGG_TRAFFIC_PER_ALG_BYTE else None,
+            "traffic_unit": "GB per step (ncu DRAM bytes per implementation byte x implementation bytes)",
+            "ms_per_step": round(agg_ms, 4), "launches_per_step": agg_launches,
+            "avg_launch_ms": round(agg_ms / agg_launches, 5) if agg_launches else None}
+        step_ms = headline["total_ms"] / args.steps
+        gbs = tot_alg / (step_ms / 1e3) / 1e9
+        out["pipeline_roofline"] = {"alg_bytes_per_pair_mb": {("census" if c == CENSUS else "bt"):
+                                                              round(per_pair[c]["total"] / 1e6, 1) for c in per_pair},
+                                    "achieved": round(gbs, 1), "unit": "GB/s", "frac": round(gbs / pk["hbm_gbs"], 4)}
+        out["kernels_ms_per_step"] = {k: round(v["ms"] / ps, 4) for k, v in prof.items() if v["launches"]}
         out["kernels_hbm"] = stage_bandwidth(prof, pk["hbm_gbs"])
     else:
         out["impl"] = "reference"

@@ -111,6 +111,8 @@ _SIGS = {
     "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
     "pyrsgm_gb300_set_packed_words": (_i, [_i]),
     "pyrsgm_gb300_set_autotune": (_i, [_i]),
+    "pyrsgm_gb300_set_fused": (_i, [_i]),
+    "pyrsgm_gb300_fused_stalls": (C.c_uint, [_i]),
     "pyrsgm_gb300_autotune_entries": (_i, [_vp, _i]),
     "pyrsgm_gb300_autotune_clear": (None, []),
     "pyrsgm_gb300_read_pfm": (_i, [C.c_char_p, _vp, _sz, C.POINTER(_i), C.POINTER(_i), C.c_char_p, _sz]),

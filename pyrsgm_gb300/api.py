@@ -213,6 +213,17 @@ def set_packed_words(words: int) -> int:
     return r
 
 
+def set_fused(on: bool) -> bool:
+    """Fused aggregation passes for the 16-label pyramid levels
+    (pyrsgm_gb300_set_fused); returns the previous setting."""
+    return bool(lib().pyrsgm_gb300_set_fused(1 if on else 0))
+
+
+def fused_stalls(reset: bool = False) -> int:
+    """Waits of the fused pass that ran out of time (pyrsgm_gb300_fused_stalls)."""
+    return int(lib().pyrsgm_gb300_fused_stalls(1 if reset else 0))
+
+
 def set_autotune(on: bool) -> bool:
     """Measure the 16/32/64-label kernel shape per launch key on the batch
     engine's first run of each new batch (pyrsgm_gb300_set_autotune);

@@ -42,6 +42,12 @@ static const int g_packed_wps = [] {
 }();
 int packed_min_warps_per_sm() { return g_packed_wps; }
 
+static std::atomic<int> g_fused{[] {
+    const char* e = std::getenv("PYRSGM_GB300_FUSED");
+    return e ? (std::atoi(e) != 0 ? 1 : 0) : 1;
+}()};
+int fused_mode() { return g_fused.load(std::memory_order_relaxed); }
+
 static std::atomic<int> g_autotune{[] {
     const char* e = std::getenv("PYRSGM_GB300_AUTOTUNE");
     return e && std::atoi(e) != 0 ? 1 : 0;
@@ -422,6 +428,8 @@ int pyrsgm_gb300_set_packed_words(int words)
     if (words != 0 && words != 2 && words != 4 && words != 8) return -1;
     return pg::g_packed_words.exchange(words, std::memory_order_relaxed);
 }
+
+int pyrsgm_gb300_set_fused(int on) { return pg::g_fused.exchange(on ? 1 : 0, std::memory_order_relaxed); }
 
 int pyrsgm_gb300_set_autotune(int on) { return pg::g_autotune.exchange(on ? 1 : 0, std::memory_order_relaxed); }
 

@@ -43,6 +43,7 @@
 #include "sgm_common.cuh"
 #include "sgm_launch.h"
 #include "k_paths_packed.cuh"
+#include "k_fused.cuh"
 
 namespace pg {
 
@@ -819,11 +820,18 @@ cudaError_t launch_paths_mode(const Jobs<NJ>& jobs, const LevelExtent& e, cudaSt
     long long rows = 0;
     for (int i = 0; i < jobs.n; ++i) rows += jobs.d[i].h;
     const int D = jobs.d[0].D;
-    const TuneKey key{D, PYR ? 1 : 0, (int)std::min<long long>(rows, INT_MAX), e.max_w};
+    // 16-label pyramid levels with all three paths: the wide shape is the
+    // fused T->B + L->R and R->L + WTA passes (k_fused.cuh)
+    bool fused = false;
+    if constexpr (PYR) fused = D == 16 && fused_mode() != 0 && fused_applicable(jobs);
+    const TuneKey key{D, PYR ? (fused ? 2 : 1) : 0, (int)std::min<long long>(rows, INT_MAX), e.max_w};
     cudaError_t err = cudaSuccess;
     switch (path_variant(D)) {
     case 10016: {
         auto run = [&](int nw) {
+            if constexpr (PYR) {
+                if (nw == 8 && fused) return launch_paths_fused16<NJ>(jobs, e, st);
+            }
             return nw == 8 ? launch_paths_packed<8, 1, PYR, NJ>(jobs, e, st)
                            : launch_paths_packed<2, 4, PYR, NJ>(jobs, e, st);
         };

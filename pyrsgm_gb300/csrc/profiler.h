@@ -16,6 +16,8 @@ enum ProfKind {
     PK_POST = 6,
     PK_P2TABLE = 7,
     PK_WTA = 8,
+    PK_TBLR = 9,   // fused T->B + L->R pass (16-label pyramid levels)
+    PK_RLW = 10,   // fused R->L + winner-take-all pass
     PK_COUNT
 };
 

@@ -86,17 +86,32 @@ def test_p2_table_matches_libm_closely():
 PACKED = [c for c in cases.SINGLE_SCALE + cases.LEVELS if c["D"] in (16, 32, 64)]
 
 
-@pytest.mark.parametrize("words", [8, 2])
-@pytest.mark.parametrize("case", PACKED, ids=[c["name"] for c in PACKED])
-def test_packed_shapes_match_reference(case, words):
-    """Both shapes of the 16/32/64-label kernels (one thread per 16 labels,
-    or a chain spread over several threads) give the reference's results."""
+# kernel shapes of the 16/32/64-label aggregation: (words per thread, fused
+# passes for 16-label pyramid levels)
+SHAPES = [(8, True), (8, False), (2, True)]
+SHAPE_IDS = ["wide_fused", "wide", "spread"]
+
+
+def _run_shape(case, words, fused):
     import pyrsgm_gb300 as pg
     prev = pg.set_packed_words(words)
+    prev_f = pg.set_fused(fused)
     try:
-        mine = _runners.run_mine(case)
+        return _runners.run_mine(case)
     finally:
         pg.set_packed_words(prev)
+        pg.set_fused(prev_f)
+
+
+@pytest.mark.parametrize("words,fused", SHAPES, ids=SHAPE_IDS)
+@pytest.mark.parametrize("case", PACKED, ids=[c["name"] for c in PACKED])
+def test_packed_shapes_match_reference(case, words, fused):
+    """Every shape of the 16/32/64-label kernels (one thread per 16 labels,
+    the fused two-pass form of the 16-label pyramid levels, or a chain spread
+    over several threads) gives the reference's results."""
+    import pyrsgm_gb300 as pg
+    mine = _run_shape(case, words, fused)
+    assert pg.fused_stalls() == 0
     if _oracle.ref_available():
         other = _runners.run_ref(case)
     else:
@@ -119,15 +134,10 @@ ODD_PACKED = [
 ]
 
 
-@pytest.mark.parametrize("words", [8, 2])
+@pytest.mark.parametrize("words,fused", SHAPES, ids=SHAPE_IDS)
 @pytest.mark.parametrize("case", ODD_PACKED, ids=[c["name"] for c in ODD_PACKED])
-def test_packed_shapes_odd_widths_match_reference(case, words):
-    import pyrsgm_gb300 as pg
-    prev = pg.set_packed_words(words)
-    try:
-        mine = _runners.run_mine(case)
-    finally:
-        pg.set_packed_words(prev)
+def test_packed_shapes_odd_widths_match_reference(case, words, fused):
+    mine = _run_shape(case, words, fused)
     if _oracle.ref_available():
         other = _runners.run_ref(case)
     else:
