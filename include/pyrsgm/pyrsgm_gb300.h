@@ -215,8 +215,8 @@ int pyrsgm_gb300_filter_speckles(short* d_disp, size_t pitch_bytes, int width, i
  * PYRSGM_GB300_PACKED_NW gives the initial setting. */
 int pyrsgm_gb300_set_packed_words(int words);
 
-/* Fused aggregation of the 16-label pyramid levels with three paths (on by
- * default; PYRSGM_GB300_FUSED=0 turns it off at load).  When on, the wide
+/* Fused aggregation of the 16-label pyramid levels with three paths (off by
+ * default; PYRSGM_GB300_FUSED=1 turns it on at load).  When on, the wide
  * shape of those levels is two passes -- top-to-bottom and left-to-right
  * together on a skewed front of 32-row bands (each band waits, bounded, for
  * the band above's bottom edge), then right-to-left with the

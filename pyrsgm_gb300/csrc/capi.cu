@@ -44,7 +44,7 @@ int packed_min_warps_per_sm() { return g_packed_wps; }
 
 static std::atomic<int> g_fused{[] {
     const char* e = std::getenv("PYRSGM_GB300_FUSED");
-    return e ? (std::atoi(e) != 0 ? 1 : 0) : 1;
+    return e && std::atoi(e) != 0 ? 1 : 0;
 }()};
 int fused_mode() { return g_fused.load(std::memory_order_relaxed); }
 
