@@ -14,9 +14,7 @@ constexpr uint32_t kBtBias2 = 0x01000100u;   // 256 in each 16-bit half
 
 // ---------------------------------------------------------------------------
 // pyrDown: 5x5 [1 4 6 4 1]^2 / 256, BORDER_REFLECT_101, (sum+128)>>8.
-// Reference: src/pyrdown.cu:16-52.  One block computes a 32x8 output tile
-// from a shared 67x19 source tile (coalesced row loads, reflected indices
-// resolved once at load time).
+// Reference: src/pyrdown.cu:16-52.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int reflect101(int i, int n)
 {
@@ -25,36 +23,78 @@ __device__ __forceinline__ int reflect101(int i, int n)
     return i < 0 ? 0 : i;
 }
 
-constexpr int kPdTx = 32, kPdTy = 8;
-constexpr int kPdSw = 2 * kPdTx + 3, kPdSh = 2 * kPdTy + 3;
+// One block: 128 x 16 output pixels, a thread per 4 adjacent outputs of a
+// row.  The source tile (rows 2*y0 - 2 .. 2*y0 + 32, columns 2*x0 - 4 ..
+// 2*x0 + 259, word aligned) is staged as words when it lies inside the
+// image and the rows are word aligned, else byte by byte with reflected
+// indices.  Each thread sums the five taps of its 11 source columns
+// vertically, then the five horizontal taps of each output.
+constexpr int kPdX = 128, kPdY = 16;
+constexpr int kPdSWB = 2 * kPdX + 8;    // staged source bytes per row
+constexpr int kPdSWW = kPdSWB / 4;
+constexpr int kPdSH = 2 * kPdY + 3;     // staged source rows
 
 template <int NB>
 __global__ void __launch_bounds__(256) k_pyrdown(const __grid_constant__ PyrDownBatch<NB> b)
 {
     const PyrDownDesc& P = b.d[blockIdx.z];
-    const int x0 = blockIdx.x * kPdTx, y0 = blockIdx.y * kPdTy;
+    const int x0 = blockIdx.x * kPdX, y0 = blockIdx.y * kPdY;
     if (x0 >= P.dw || y0 >= P.dh) return;
-    __shared__ uint8_t tile[kPdSh][kPdSw + 1];
-    const int sx0 = 2 * x0 - 2, sy0 = 2 * y0 - 2;
-    for (int i = threadIdx.x; i < kPdSh * kPdSw; i += blockDim.x) {
-        const int r = i / kPdSw, c = i - r * kPdSw;
-        const int sy = reflect101(sy0 + r, P.sh), sx = reflect101(sx0 + c, P.sw);
-        tile[r][c] = P.src[(size_t)sy * P.sstep + sx];
+    __shared__ uint32_t tw[kPdSH][kPdSWW];   // byte c of row r: source (reflect(2*y0 - 2 + r), reflect(2*x0 - 4 + c))
+    const int sx0 = 2 * x0 - 4, sy0 = 2 * y0 - 2;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(P.src) | (uintptr_t)P.sstep) & 3u) == 0;
+    if (aligned && sx0 >= 0 && sx0 + kPdSWB <= P.sw && sy0 >= 0 && sy0 + kPdSH <= P.sh) {
+        for (int i = threadIdx.x; i < kPdSH * kPdSWW; i += 256) {
+            const int r = i / kPdSWW, k = i - r * kPdSWW;
+            tw[r][k] = __ldg(reinterpret_cast<const uint32_t*>(P.src + (size_t)(sy0 + r) * P.sstep + sx0) + k);
+        }
+    } else {
+        uint8_t* tb = reinterpret_cast<uint8_t*>(&tw[0][0]);
+        for (int i = threadIdx.x; i < kPdSH * kPdSWB; i += 256) {
+            const int r = i / kPdSWB, c = i - r * kPdSWB;
+            tb[i] = __ldg(P.src + (size_t)reflect101(sy0 + r, P.sh) * P.sstep + reflect101(sx0 + c, P.sw));
+        }
     }
     __syncthreads();
-    const int tx = threadIdx.x & (kPdTx - 1), ty = threadIdx.x / kPdTx;
-    const int x = x0 + tx, y = y0 + ty;
-    if (x >= P.dw || y >= P.dh) return;
-    const int w5[5] = {1, 4, 6, 4, 1};
-    int sum = 0;
+    const int tx = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int xb = x0 + 4 * tx;
+    if (xb >= P.dw) return;
+    const int np = imin(4, P.dw - xb);
+#pragma unroll 1
+    for (int ty = warp; ty < kPdY; ty += 8) {
+        const int y = y0 + ty;
+        if (y >= P.dh) break;
+        // vertical taps of source columns 2*xb - 2 .. 2*xb + 8 (tile bytes 8*tx + 2 .. 8*tx + 12)
+        int v[11];
 #pragma unroll
-    for (int ky = 0; ky < 5; ++ky) {
-        int rs = 0;
+        for (int k = 0; k < 11; ++k) v[k] = 0;
+        const int w5[5] = {1, 4, 6, 4, 1};
 #pragma unroll
-        for (int kx = 0; kx < 5; ++kx) rs += w5[kx] * (int)tile[2 * ty + ky][2 * tx + kx];
-        sum += w5[ky] * rs;
+        for (int ky = 0; ky < 5; ++ky) {
+            const uint32_t* row = tw[2 * ty + ky] + 2 * tx;
+            const uint32_t q0 = row[0], q1 = row[1], q2 = row[2], q3 = row[3];
+#pragma unroll
+            for (int k = 0; k < 11; ++k) {
+                const int bi = k + 2;
+                const uint32_t q = bi < 4 ? q0 : bi < 8 ? q1 : bi < 12 ? q2 : q3;
+                v[k] += w5[ky] * (int)((q >> (8 * (bi & 3))) & 0xffu);
+            }
+        }
+        uint32_t out = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int sum = v[2 * j] + 4 * v[2 * j + 1] + 6 * v[2 * j + 2] + 4 * v[2 * j + 3] + v[2 * j + 4];
+            out |= (uint32_t)((sum + 128) >> 8) << (8 * j);
+        }
+        uint8_t* dst = P.dst + (size_t)y * P.dstep + xb;
+        if (np == 4 && (reinterpret_cast<uintptr_t>(dst) & 3u) == 0) {
+            *reinterpret_cast<uint32_t*>(dst) = out;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j < np) dst[j] = (uint8_t)(out >> (8 * j));
+        }
     }
-    P.dst[(size_t)y * P.dstep + x] = (uint8_t)((sum + 128) >> 8);
 }
 
 // ---------------------------------------------------------------------------
@@ -67,9 +107,41 @@ __global__ void __launch_bounds__(256) k_pyrdown(const __grid_constant__ PyrDown
 // store their 25-bit descriptor as one word per pixel; BT pixels store four
 // words of 16-bit pairs (gradient low half, intensity high half):
 // value + 256, value, lo + 256, hi — the operands of bt_pixel().
+//
+// The view-0 blocks also start the level: every pixel's disp2 key is
+// cleared, and on refine levels the label base is derived from the parent
+// level (kernel_PrepareRefineLabels, src/sgm_kernels.cu:955-1000; a
+// rejected parent -- invalid disparity or confidence below the minimum --
+// becomes kNoParent: every label of the pixel is invalid).
+//
+// One block: 128 x 16 pixels of one view, a thread per 4 adjacent pixels
+// of a row.  The image tile with its 2-pixel border (4 columns on each
+// side, so rows stay word aligned) is staged as words when it lies inside
+// the image and the rows are word aligned, else byte by byte with
+// replicated borders.
 // ---------------------------------------------------------------------------
-constexpr int kFtX = 32, kFtY = 8, kFtHalo = 2;
-constexpr int kFtW = kFtX + 2 * kFtHalo, kFtH = kFtY + 2 * kFtHalo;
+constexpr int kFtX = 128, kFtY = 16;
+constexpr int kFtSWB = kFtX + 8;        // staged bytes per row: image columns x0 - 4 .. x0 + 131
+constexpr int kFtSWW = kFtSWB / 4;      // ... as words
+constexpr int kFtSH = kFtY + 4;         // staged rows: y0 - 2 .. y0 + 17
+
+__device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
+
+// Label base of pixel x from its parent (the body of
+// kernel_PrepareRefineLabels).
+__device__ __forceinline__ int16_t refine_base(const LevelDesc& J, int x, int raw, float conf)
+{
+    const int16_t pinv = (int16_t)((J.minD - 1) * 16);
+    if (raw == pinv || conf < J.minConf) return kNoParent;
+    const int pred16 = raw * 2;
+    const int center = (pred16 + 8) >> 4;
+    const int resid = pred16 - center * 16;
+    int base = center + (resid < 0 ? -(J.D / 2) : -(J.D / 2) + 1);
+    const int physMax = imin(J.maxD, x);
+    const int largest = physMax - J.D + 1;
+    base = largest >= J.minD ? imin(imax(base, J.minD), largest) : J.minD;
+    return (int16_t)base;
+}
 
 template <int NJ>
 __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<NJ> jobs)
@@ -83,82 +155,148 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
     uint4* feat = view ? J.featR : J.featL;
     const int W = J.w, H = J.h;
 
-    __shared__ uint8_t t[kFtH][kFtW];
-    for (int i = threadIdx.x; i < kFtH * kFtW; i += blockDim.x) {
-        const int r = i / kFtW, c = i - r * kFtW;
-        t[r][c] = img[(size_t)iclamp(y0 - kFtHalo + r, 0, H - 1) * step + iclamp(x0 - kFtHalo + c, 0, W - 1)];
+    __shared__ uint32_t tw[kFtSH][kFtSWW];   // byte c of row r: image pixel (y0 - 2 + r, x0 - 4 + c), clamped
+    const bool aligned = ((reinterpret_cast<uintptr_t>(img) | (uintptr_t)step) & 3u) == 0;
+    if (aligned && x0 >= 4 && x0 + kFtX + 4 <= W && y0 >= 2 && y0 + kFtY + 2 <= H) {
+        for (int i = threadIdx.x; i < kFtSH * kFtSWW; i += 256) {
+            const int r = i / kFtSWW, k = i - r * kFtSWW;
+            tw[r][k] = __ldg(reinterpret_cast<const uint32_t*>(img + (size_t)(y0 - 2 + r) * step + x0 - 4) + k);
+        }
+    } else {
+        uint8_t* tb = reinterpret_cast<uint8_t*>(&tw[0][0]);
+        for (int i = threadIdx.x; i < kFtSH * kFtSWB; i += 256) {
+            const int r = i / kFtSWB, c = i - r * kFtSWB;
+            tb[i] = __ldg(img + (size_t)iclamp(y0 - 2 + r, 0, H - 1) * step + iclamp(x0 - 4 + c, 0, W - 1));
+        }
     }
     __syncthreads();
-    const int tx = threadIdx.x & (kFtX - 1), ty = threadIdx.x / kFtX;
-    const int x = x0 + tx, y = y0 + ty;
-    if (x >= W || y >= H) return;
-    // Tile entry (ty + 2 + dy, tx + 2 + dx) holds pixel (clamp(y + dy),
-    // clamp(x + dx)): the replicate-border neighbours need no clamping here.
-    const size_t p = (size_t)y * W + x;
-    if (J.cost == COST_CENSUS) {
-        const int c = t[ty + 2][tx + 2];
-        uint32_t cv = 0;
+    const int tx = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int xb = x0 + 4 * tx;
+    if (xb >= W) return;
+    const int np = imin(4, W - xb);                 // pixels of this thread inside the image
+    const bool vec = np == 4 && (W & 3) == 0;       // 16-byte stores of 4 words / 8-byte of 4 int16
+    const int ftzero = imax(J.pfc, 15) | 1;
+#pragma unroll 1
+    for (int rr = warp; rr < kFtY; rr += 8) {
+        const int y = y0 + rr;
+        if (y >= H) break;
+        const size_t p = (size_t)y * W + xb;
+        if (J.cost == COST_CENSUS) {
+            // bit (dy, dx) of the 4 pixels at once: bytes 2 + dx .. 5 + dx of
+            // the 12-byte row window, compared with the 4 centre bytes
+            const uint32_t ctr = tw[rr + 2][tx + 1];
+            const uint32_t ctr7 = ctr & 0x7f7f7f7fu;
+            uint32_t acc[4] = {0u, 0u, 0u, 0u};   // 8 bits per byte lane, first bit highest
+            int pos = 0;
 #pragma unroll
-        for (int dy = 0; dy < 5; ++dy) {
+            for (int dy = 0; dy < 5; ++dy) {
+                const uint32_t w0 = tw[rr + dy][tx], w1 = tw[rr + dy][tx + 1], w2 = tw[rr + dy][tx + 2];
+                const uint32_t n[5] = {__funnelshift_r(w0, w1, 16), __funnelshift_r(w0, w1, 24), w1,
+                                       __funnelshift_r(w1, w2, 8), __funnelshift_r(w1, w2, 16)};
 #pragma unroll
-            for (int dx = 0; dx < 5; ++dx) cv = (cv << 1) | (uint32_t)(t[ty + dy][tx + dx] < c);
+                for (int dx = 0; dx < 5; ++dx, ++pos) {
+                    // unsigned a < b per byte (SWAR): the low seven bits by a
+                    // subtraction that cannot borrow across bytes, then the top bits
+                    const uint32_t a = n[dx];
+                    const uint32_t d = (a | 0x80808080u) - ctr7;
+                    const uint32_t lt = ((~a & ctr) | (~(a ^ ctr) & ~d)) & 0x80808080u;
+                    acc[pos >> 3] = (acc[pos >> 3] << 1) | (lt >> 7);
+                }
+            }
+            uint32_t cv[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                cv[j] = (byte_of(acc[0], j) << 17) | (byte_of(acc[1], j) << 9) | (byte_of(acc[2], j) << 1) |
+                        byte_of(acc[3], j);
+            uint32_t* out = reinterpret_cast<uint32_t*>(feat) + p;
+            if (vec) {
+                *reinterpret_cast<uint4*>(out) = make_uint4(cv[0], cv[1], cv[2], cv[3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (j < np) out[j] = cv[j];
+            }
+        } else {
+            // bytes 2 .. 9 of the window rows rr + 1 .. rr + 3: columns xb - 2 .. xb + 5
+            uint32_t r1[8], r2[8], r3[8];
+            {
+                const uint32_t a0 = tw[rr + 1][tx], a1 = tw[rr + 1][tx + 1], a2 = tw[rr + 1][tx + 2];
+                const uint32_t b0 = tw[rr + 2][tx], b1 = tw[rr + 2][tx + 1], b2 = tw[rr + 2][tx + 2];
+                const uint32_t c0 = tw[rr + 3][tx], c1 = tw[rr + 3][tx + 1], c2 = tw[rr + 3][tx + 2];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int bi = k + 2;   // byte index in the 12-byte window
+                    const uint32_t wa = bi < 4 ? a0 : bi < 8 ? a1 : a2;
+                    const uint32_t wb = bi < 4 ? b0 : bi < 8 ? b1 : b2;
+                    const uint32_t wc = bi < 4 ? c0 : bi < 8 ? c1 : c2;
+                    r1[k] = byte_of(wa, bi & 3);
+                    r2[k] = byte_of(wb, bi & 3);
+                    r3[k] = byte_of(wc, bi & 3);
+                }
+            }
+            // g[i]: gradient at pixel column xb - 1 + i (window byte k = i + 1)
+            int g[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                const int k = i + 1;
+                int v = ((int)r2[k + 1] - (int)r2[k - 1]) * 2;
+                v += (int)r1[k + 1] - (int)r1[k - 1];
+                v += (int)r3[k + 1] - (int)r3[k - 1];
+                g[i] = iclamp(v, -ftzero, ftzero) + ftzero;
+            }
+            auto interval = [](int v, int l, int r, uint32_t& lo, uint32_t& hi) {
+                const int vl = (v + l) >> 1, vr = (v + r) >> 1;
+                lo = (uint32_t)imin(imin(vl, vr), v);
+                hi = (uint32_t)imax(imax(vl, vr), v);
+            };
+            uint4 f[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                // the neighbour columns are clamped first (x - 1 -> 0 at the left border)
+                const int x = xb + j;
+                const bool hl = x > 0, hr = x + 1 < W;
+                const int gv = g[j + 1], iv = (int)r2[j + 2];
+                uint32_t glo, ghi, ilo, ihi;
+                interval(gv, hl ? g[j] : gv, hr ? g[j + 2] : gv, glo, ghi);
+                interval(iv, hl ? (int)r2[j + 1] : iv, hr ? (int)r2[j + 3] : iv, ilo, ihi);
+                const uint32_t X = (uint32_t)gv | ((uint32_t)iv << 16), X0 = glo | (ilo << 16), X1 = ghi | (ihi << 16);
+                f[j] = make_uint4(X + kBtBias2, X, X0 + kBtBias2, X1);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j < np) feat[p + j] = f[j];
         }
-        reinterpret_cast<uint32_t*>(feat)[p] = cv;
-    } else {
-        const int ftzero = imax(J.pfc, 15) | 1;
-        // gradient at tile column c of row y (its neighbours clamped to the image)
-        auto grad = [&](int c) -> int {
-            int g = (t[ty + 2][c + 1] - t[ty + 2][c - 1]) * 2;
-            g += t[ty + 1][c + 1] - t[ty + 1][c - 1];
-            g += t[ty + 3][c + 1] - t[ty + 3][c - 1];
-            return iclamp(g, -ftzero, ftzero) + ftzero;
-        };
-        // value, lo, hi of one channel as 16-bit fields
-        auto interval = [](int v, int l, int r, uint32_t& lo, uint32_t& hi) {
-            const int vl = (v + l) / 2, vr = (v + r) / 2;
-            lo = (uint32_t)imin(imin(vl, vr), v);
-            hi = (uint32_t)imax(imax(vl, vr), v);
-        };
-        // the neighbour columns are clamped first (x - 1 -> 0 at the left border)
-        const int cc = tx + 2, cm = x > 0 ? cc - 1 : cc, cq = x + 1 < W ? cc + 1 : cc;
-        const int gv = grad(cc), iv = t[ty + 2][cc];
-        uint32_t glo, ghi, ilo, ihi;
-        interval(gv, grad(cm), grad(cq), glo, ghi);
-        interval(iv, t[ty + 2][cm], t[ty + 2][cq], ilo, ihi);
-        const uint32_t X = (uint32_t)gv | ((uint32_t)iv << 16), X0 = glo | (ilo << 16), X1 = ghi | (ihi << 16);
-        feat[p] = make_uint4(X + kBtBias2, X, X0 + kBtBias2, X1);
+        if (view == 0) {
+            if (vec) {
+                *reinterpret_cast<uint4*>(J.keys + p) = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (j < np) J.keys[p + j] = 0xffffffffu;   // no disp2 candidate yet
+            }
+            if (J.refine) {
+                const int py = imin(y >> 1, J.ph - 1);
+                const int16_t* prow = J.pdisp + (size_t)py * J.pd_pitch;
+                const float* crow = J.pconf + (size_t)py * J.pc_pitch;
+                int16_t b[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int px = imin((xb + j) >> 1, J.pw - 1);
+                    b[j] = j < np ? refine_base(J, xb + j, __ldg(prow + px), __ldg(crow + px)) : (int16_t)0;
+                }
+                int16_t* bo = J.base + p;
+                if (vec) {
+                    *reinterpret_cast<uint2*>(bo) =
+                        make_uint2((uint32_t)(uint16_t)b[0] | ((uint32_t)(uint16_t)b[1] << 16),
+                                   (uint32_t)(uint16_t)b[2] | ((uint32_t)(uint16_t)b[3] << 16));
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (j < np) bo[j] = b[j];
+                }
+            }
+        }
     }
-    if (view == 0) J.keys[p] = 0xffffffffu;  // no disp2 candidate yet
-}
-
-// ---------------------------------------------------------------------------
-// Refine labels: kernel_PrepareRefineLabels, src/sgm_kernels.cu:955-1000.
-// A rejected parent (invalid disparity or confidence below the minimum)
-// becomes kNoParent: every label of the pixel is invalid (valid_mask = 0).
-// ---------------------------------------------------------------------------
-template <int NJ>
-__global__ void __launch_bounds__(256) k_refine_labels(const __grid_constant__ Jobs<NJ> jobs)
-{
-    const LevelDesc& J = jobs.d[blockIdx.z];
-    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (!J.refine || x >= J.w || y >= J.h) return;
-    const int px = imin(x >> 1, J.pw - 1), py = imin(y >> 1, J.ph - 1);
-    const int16_t raw = J.pdisp[(size_t)py * J.pd_pitch + px];
-    const float conf = J.pconf[(size_t)py * J.pc_pitch + px];
-    const int16_t pinv = (int16_t)((J.minD - 1) * 16);
-    int16_t out = kNoParent;
-    if (!(raw == pinv || conf < J.minConf)) {
-        const int pred16 = (int)raw * 2;
-        const int center = (pred16 + 8) >> 4;
-        const int resid = pred16 - center * 16;
-        int base = center + (resid < 0 ? -(J.D / 2) : -(J.D / 2) + 1);
-        const int physMax = imin(J.maxD, x);
-        const int largest = physMax - J.D + 1;
-        base = largest >= J.minD ? imin(imax(base, J.minD), largest) : J.minD;
-        out = (int16_t)base;
-    }
-    J.base[(size_t)y * J.w + x] = out;
 }
 
 // ---------------------------------------------------------------------------
@@ -529,7 +667,7 @@ __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ J
 template <int NB>
 cudaError_t launch_pyrdown(const PyrDownBatch<NB>& b, int max_dw, int max_dh, cudaStream_t st)
 {
-    dim3 grid((max_dw + kPdTx - 1) / kPdTx, (max_dh + kPdTy - 1) / kPdTy, b.n);
+    dim3 grid((max_dw + kPdX - 1) / kPdX, (max_dh + kPdY - 1) / kPdY, b.n);
     prof_begin(st);
     k_pyrdown<NB><<<grid, 256, 0, st>>>(b);
     count_launch();
@@ -560,18 +698,18 @@ cudaError_t launch_prepare(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStrea
     prof_begin(st);
     k_features<NJ><<<gf, 256, 0, st>>>(jobs);
     count_launch();
-    prof_end(PK_FEATURES, jobs_px(jobs) * 2 * (1 + (jobs.d[0].cost == COST_CENSUS ? 4 : 16)), st);  // read u8, write features, both views
-    cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) return err;
-    if (e.any_refine) {
-        dim3 gl((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
-        prof_begin(st);
-        k_refine_labels<NJ><<<gl, 256, 0, st>>>(jobs);
-        count_launch();
-        prof_end(PK_LABELS, jobs_px(jobs) * (2 + 6.0 / 4), st);  // write base, read the 1/4-size parent
-        err = cudaGetLastError();
+    if (prof_enabled()) {
+        // read u8 and write features of both views, write the keys; refine
+        // levels read the quarter-size parent and write the label base
+        double by = 0;
+        for (int i = 0; i < jobs.n; ++i) {
+            const LevelDesc& d = jobs.d[i];
+            const double px = (double)d.w * d.h;
+            by += px * (2 * (1 + (d.cost == COST_CENSUS ? 4 : 16)) + 4 + (d.refine ? 2 + 6.0 / 4 : 0));
+        }
+        prof_end(PK_FEATURES, by, st);
     }
-    return err;
+    return cudaGetLastError();
 }
 
 // All jobs in `jobs` share the cost mode and the refine flag.

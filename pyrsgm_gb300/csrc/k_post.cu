@@ -29,32 +29,38 @@ cudaError_t launch_paths(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_
     return jobs.d[0].pyr ? launch_paths_mode<true, NJ>(jobs, e, st) : launch_paths_mode<false, NJ>(jobs, e, st);
 }
 
-// Median of nine by 19 compare-exchanges (the opt_med9 network of
-// Paeth / Devillard, "Fast median search: an ANSI C implementation").
-__device__ __forceinline__ void cx(int& a, int& b)
+// 3x3 median of the interior by column sorts: each column of three is
+// sorted once and shared by the three windows it belongs to; the median of
+// the nine is the median of (largest column minimum, median of the column
+// medians, smallest column maximum) -- the structure of the opt_med9
+// network of Paeth / Devillard ("Fast median search: an ANSI C
+// implementation").
+__device__ __forceinline__ int med3(int a, int b, int c) { return imax(imin(a, b), imin(imax(a, b), c)); }
+
+struct Col3 {
+    int lo, mid, hi;
+};
+__device__ __forceinline__ Col3 sort3(int a, int b, int c)
 {
-    const int t = imin(a, b);
-    b = imax(a, b);
-    a = t;
+    const int l = imin(a, b), h = imax(a, b);
+    return {imin(l, c), imax(l, imin(h, c)), imax(h, c)};
 }
-__device__ __forceinline__ int median9(int p0, int p1, int p2, int p3, int p4, int p5, int p6, int p7, int p8)
+__device__ __forceinline__ int median9(const Col3& a, const Col3& b, const Col3& c)
 {
-    cx(p1, p2); cx(p4, p5); cx(p7, p8); cx(p0, p1); cx(p3, p4); cx(p6, p7);
-    cx(p1, p2); cx(p4, p5); cx(p7, p8); cx(p0, p3); cx(p5, p8); cx(p4, p7);
-    cx(p3, p6); cx(p1, p4); cx(p2, p5); cx(p4, p7); cx(p4, p2); cx(p6, p4);
-    cx(p4, p2);
-    return p4;
+    return med3(imax(imax(a.lo, b.lo), c.lo), med3(a.mid, b.mid, c.mid), imin(imin(a.hi, b.hi), c.hi));
 }
 
-// One block: 32 x 8 pixels.  The (LR-checked) disparities of the tile and
-// its one-pixel halo are computed once into shared memory, then each thread
-// takes the median of its 3x3 neighbourhood (the in-image neighbours only,
-// sorted, middle element, at the image border).
+// One block: 128 x 16 pixels, a thread per 4 adjacent pixels of a row.  The
+// (LR-checked) disparities of the tile and its one-pixel halo are computed
+// once into shared memory; the median takes the in-image neighbours only
+// (sorted, middle element) at the image border.
+constexpr int kPoX = 128, kPoY = 16;
+
 template <int NJ>
 __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> jobs)
 {
     const LevelDesc& J = jobs.d[blockIdx.z];
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
+    const int x0 = blockIdx.x * kPoX, y0 = blockIdx.y * kPoY;
     if (x0 >= J.w || y0 >= J.h) return;
     const int W = J.w, H = J.h;
     const int16_t inv = (int16_t)((J.minD - 1) * 16);
@@ -68,7 +74,7 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
         if (!check || d16 == inv) return d16;
         const unsigned* krow = J.keys + (size_t)yy * W;
         auto disp2 = [&](int rx) -> int {
-            const unsigned k = krow[rx];
+            const unsigned k = __ldg(krow + rx);
             return k == 0xffffffffu ? (int)inv : (int)(0xffffu - (k & 0xffffu)) - rx;
         };
         const int d0 = d16 >> 4, d1 = (d16 + 15) >> 4;
@@ -76,7 +82,10 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
         if (J.pyr) {
             bool ok = false;
             if (r0 >= 0 && r0 < W) { const int v = disp2(r0); if (v >= J.minD && abs(v - d0) <= J.maxdiff) ok = true; }
-            if (r1 >= 0 && r1 < W) { const int v = disp2(r1); if (v >= J.minD && abs(v - d1) <= J.maxdiff) ok = true; }
+            if (!ok && r1 != r0 && r1 >= 0 && r1 < W) {
+                const int v = disp2(r1);
+                if (v >= J.minD && abs(v - d1) <= J.maxdiff) ok = true;
+            }
             return ok ? d16 : (int)inv;
         }
         bool bad0 = false, bad1 = false;
@@ -84,63 +93,118 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
         if (r1 >= 0 && r1 < W) { const int v = disp2(r1); bad1 = v >= J.minD && abs(v - d1) > J.maxdiff; }
         return (bad0 && bad1) ? (int)inv : d16;
     };
-    __shared__ int16_t td[10][34];
+    __shared__ int16_t td[kPoY + 2][kPoX + 2];   // row r, column c: pixel (y0 - 1 + r, x0 - 1 + c)
     if (check || med) {
-        for (int i = threadIdx.x; i < 10 * 34; i += blockDim.x) {
-            const int r = i / 34, c = i - r * 34;
+        for (int i = threadIdx.x; i < (kPoY + 2) * (kPoX + 2); i += blockDim.x) {
+            const int r = i / (kPoX + 2), c = i - r * (kPoX + 2);
             const int yy = y0 - 1 + r, xx = x0 - 1 + c;
             td[r][c] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? (int16_t)disp_at(xx, yy) : inv;
         }
         __syncthreads();
     }
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int x = x0 + tx, y = y0 + ty;
-    if (x >= W || y >= H) return;
-    const size_t p = (size_t)y * W + x;
-    const int d_in = J.disp_raw[p];
-    int d = (check || med) ? (int)td[ty + 1][tx + 1] : d_in;
-    float c = (d != d_in) ? 0.0f : J.conf_raw[p];  // the check zeroes what it rejects
-    if (med) {
-        int m;
-        if (x > 0 && x + 1 < W && y > 0 && y + 1 < H) {
-            m = median9(td[ty][tx], td[ty][tx + 1], td[ty][tx + 2], td[ty + 1][tx], td[ty + 1][tx + 1],
-                        td[ty + 1][tx + 2], td[ty + 2][tx], td[ty + 2][tx + 1], td[ty + 2][tx + 2]);
-        } else {
-            int v[9];
-            int n = 0;
-            for (int dy = -1; dy <= 1; ++dy) {
-                if (y + dy < 0 || y + dy >= H) continue;
-                for (int dx = -1; dx <= 1; ++dx) {
-                    if (x + dx < 0 || x + dx >= W) continue;
-                    v[n++] = td[ty + 1 + dy][tx + 1 + dx];
+    const int tx = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int xb = x0 + 4 * tx;
+    if (xb >= W) return;
+    const int np = imin(4, W - xb);
+#pragma unroll 1
+    for (int ty = warp; ty < kPoY; ty += 8) {
+        const int y = y0 + ty;
+        if (y >= H) break;
+        const size_t p = (size_t)y * W + xb;
+        int dv[4], dn[4];
+        float cf[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int jj = imin(j, np - 1);
+            const int d_in = J.disp_raw[p + jj];
+            const int d = (check || med) ? (int)td[ty + 1][4 * tx + 1 + jj] : d_in;
+            dv[j] = d;
+            cf[j] = (d != d_in) ? 0.0f : J.conf_raw[p + jj];  // the check zeroes what it rejects
+            dn[j] = d;
+        }
+        if (med) {
+            const bool inner = xb > 0 && xb + 4 < W && y > 0 && y + 1 < H;
+            if (inner) {
+                Col3 c[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int cc = 4 * tx + k;   // tile column of pixel column xb - 1 + k
+                    c[k] = sort3(td[ty][cc], td[ty + 1][cc], td[ty + 2][cc]);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) dn[j] = median9(c[j], c[j + 1], c[j + 2]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (j >= np) break;
+                    const int x = xb + j;
+                    int v[9];
+                    int n = 0;
+                    for (int dy = -1; dy <= 1; ++dy) {
+                        if (y + dy < 0 || y + dy >= H) continue;
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            if (x + dx < 0 || x + dx >= W) continue;
+                            v[n++] = td[ty + 1 + dy][4 * tx + 1 + j + dx];
+                        }
+                    }
+                    for (int i = 1; i < n; ++i) {
+                        const int key = v[i];
+                        int q = i - 1;
+                        while (q >= 0 && v[q] > key) { v[q + 1] = v[q]; --q; }
+                        v[q + 1] = key;
+                    }
+                    dn[j] = v[n / 2];
                 }
             }
-            for (int i = 1; i < n; ++i) {
-                const int key = v[i];
-                int j = i - 1;
-                while (j >= 0 && v[j] > key) { v[j + 1] = v[j]; --j; }
-                v[j + 1] = key;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (dn[j] != dv[j]) cf[j] = 0.0f;
             }
-            m = v[n / 2];
         }
-        if (m != d) c = 0.0f;
-        d = m;
-    }
-    if (J.out16) J.out16[(size_t)y * J.out16_pitch + x] = (int16_t)d;
-    if (J.out32 && J.outc) {
-        const float f = (int16_t)d / 16.0f;
-        const bool ok = (int16_t)d != inv && f > 0.0f;
-        J.out32[(size_t)y * J.out32_pitch + x] = ok ? f : 0.0f;
-        J.outc[(size_t)y * J.outc_pitch + x] = ok ? c : 0.0f;
-    } else if (J.outc && J.conf_only_copy) {
-        J.outc[(size_t)y * J.outc_pitch + x] = c;
+        const bool vec = np == 4;
+        if (J.out16) {
+            int16_t* o = J.out16 + (size_t)y * J.out16_pitch + xb;
+            if (vec && ((reinterpret_cast<uintptr_t>(o) & 7) == 0)) {
+                *reinterpret_cast<uint2*>(o) =
+                    make_uint2((uint32_t)(uint16_t)dn[0] | ((uint32_t)(uint16_t)dn[1] << 16),
+                               (uint32_t)(uint16_t)dn[2] | ((uint32_t)(uint16_t)dn[3] << 16));
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (j < np) o[j] = (int16_t)dn[j];
+            }
+        }
+        float f32[4], fc[4];
+        const bool conv = J.out32 && J.outc;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float f = (int16_t)dn[j] / 16.0f;
+            const bool ok = (int16_t)dn[j] != inv && f > 0.0f;
+            f32[j] = ok ? f : 0.0f;
+            fc[j] = conv ? (ok ? cf[j] : 0.0f) : cf[j];
+        }
+        auto store4 = [&](float* o, const float (&v)[4]) {
+            if (vec && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
+                *reinterpret_cast<float4*>(o) = make_float4(v[0], v[1], v[2], v[3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (j < np) o[j] = v[j];
+            }
+        };
+        if (conv) {
+            store4(J.out32 + (size_t)y * J.out32_pitch + xb, f32);
+            store4(J.outc + (size_t)y * J.outc_pitch + xb, fc);
+        } else if (J.outc && J.conf_only_copy) {
+            store4(J.outc + (size_t)y * J.outc_pitch + xb, fc);
+        }
     }
 }
 
 template <int NJ>
 cudaError_t launch_post(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
-    dim3 g((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
+    dim3 g((e.max_w + kPoX - 1) / kPoX, (e.max_h + kPoY - 1) / kPoY, jobs.n);
     prof_begin(st);
     k_post<NJ><<<g, 256, 0, st>>>(jobs);
     count_launch();
