@@ -452,52 +452,83 @@ __global__ void __launch_bounds__(256) k_cost_bt_box(const __grid_constant__ Job
 // clamped pixels q, the BT cost of q at the real disparity base_p + d (255
 // when q - (base_p + d) leaves the image), clamps the sum to kMax - 1, and
 // writes kMax for a geometry-invalid label.  The sum depends on p only
-// through the window and the real disparity, so one 32x8 tile evaluates
+// through the window and the real disparity, so one 32x16 tile evaluates
 // each (window pixel, real disparity) pair once when the real disparities
 // its pixels need, [min base, max base + D - 1], span at most kTiRn:
-//   phase 1: a warp walks a window row left to right, one real disparity
-//            per lane, and keeps the running sum of the last blockSize
-//            costs (sums along x, into shared memory);
+//   phase 1: units of (window row, half row of 16 output columns, 32 real
+//            disparities) are dealt to the 8 warps in turn; a warp walks
+//            its unit's columns left to right, one real disparity per
+//            lane, keeping the running sum of the last blockSize costs
+//            (sums along x, into shared memory).  The features of a
+//            warp's next unit are copied with cp.async while it walks the
+//            current one;
 //   phase 2: a thread per pixel adds blockSize rows of those sums, two
 //            labels per 32-bit add, from its own real-disparity offset.
 // Window sums are exact integers (at most 25 * 255 here, no intermediate
-// clamp in the reference).  Tiles whose parents disagree more widely, or a
+// clamp in the reference).  Tiles whose parents disagree more widely are
+// split into two base clusters (a pass each); pixels in neither, or a
 // wider window, evaluate each window directly.
 // ---------------------------------------------------------------------------
-constexpr int kTiX = 32, kTiY = 8, kTiRn = 64, kTiMaxHalf = 2;
+constexpr int kTiX = 32, kTiY = 16, kTiRn = 64, kTiMaxHalf = 2;
+constexpr int kTiWarps = 8;
+constexpr int kTiSeg = 16;                  // output columns of a row-sum unit
 constexpr int kTiRs = kTiRn + 2;   // halves per (row, column): 33 words, odd, so columns hit distinct banks
-constexpr int kTiStage = 2 * (kTiX + 2 * kTiMaxHalf) + 32;   // staged left (SW) + right (SW + 31) features of a row unit
+constexpr int kTiStage = 2 * (kTiSeg + 2 * kTiMaxHalf) + 31;   // staged left (SW) + right (SW + 31) features of a unit
 constexpr size_t kTiHs = (size_t)(kTiY + 2 * kTiMaxHalf) * kTiX * kTiRs * 2;
-constexpr size_t kTiSmem = kTiHs + (size_t)kTiY * kTiStage * 16;
+constexpr size_t kTiSmem = kTiHs + (size_t)kTiWarps * 2 * kTiStage * 16;
 
-// Sums along x of one window row r (image row gy) for the 32 real
-// disparities rmin + r0 + lane: a running sum over the last 2*HW+1 costs.
-// The row's left features (one per window column) and the right features
-// the 32 lanes reach are first staged in the warp's shared buffer `st`.
-template <int HW>
-__device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, uint4* st, int r, int gy, int x0,
-                                            int rmin, int r0, int rn, int lane)
+__device__ __forceinline__ void tile_cp16(void* dst, const void* src)
 {
-    constexpr int SW = kTiX + 2 * HW;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void tile_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void tile_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void tile_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// A row-sum unit: window row r (image row gy), output columns x0 + cs ..
+// x0 + cs + 15, real disparities rmin + r0 .. rmin + r0 + 31.
+struct BtUnit {
+    int r, gy, cs, r0;
+};
+
+// Copy the unit's left features (one per window column, clamped) and the
+// right features its lanes reach (inside the image only) into `st`.
+template <int HW>
+__device__ __forceinline__ void bt_stage(const LevelDesc& J, uint4* st, const BtUnit& u, int x0, int rmin, int lane)
+{
+    constexpr int SW = kTiSeg + 2 * HW;
     const int W = J.w;
-    const uint4* lrow = J.featL + (size_t)gy * W;
-    const uint4* rrow = J.featR + (size_t)gy * W;
-    // right pixels gx - real for gx in [x0 - HW, x0 + 31 + HW], real in [rmin + r0, rmin + r0 + 31]
-    const int xr0 = x0 - HW - (rmin + r0 + 31);
-    uint4* sl = st;            // [SW] left, clamped columns
-    uint4* sr = st + SW;       // [SW + 31] right, from xr0
-    for (int i = lane; i < SW; i += 32) sl[i] = __ldg(&lrow[iclamp(x0 - HW + i, 0, W - 1)]);
+    const int xs = x0 + u.cs;
+    const uint4* lrow = J.featL + (size_t)u.gy * W;
+    const uint4* rrow = J.featR + (size_t)u.gy * W;
+    const int xr0 = xs - HW - (rmin + u.r0 + 31);
+    for (int i = lane; i < SW; i += 32) tile_cp16(st + i, lrow + iclamp(xs - HW + i, 0, W - 1));
     for (int i = lane; i < SW + 31; i += 32) {
         const int xx = xr0 + i;
-        if (xx >= 0 && xx < W) sr[i] = __ldg(&rrow[xx]);
+        if (xx >= 0 && xx < W) tile_cp16(st + SW + i, rrow + xx);
     }
-    __syncwarp();
-    const int ri = r0 + lane;
+}
+
+// Sums along x of one unit for its 32 real disparities: a running sum over
+// the last 2*HW+1 costs, from the staged features.
+template <int HW>
+__device__ __forceinline__ void bt_walk(const LevelDesc& J, uint16_t* hs, const uint4* st, const BtUnit& u, int x0,
+                                        int rmin, int rn, int lane)
+{
+    constexpr int SW = kTiSeg + 2 * HW;
+    const int W = J.w;
+    const int xs = x0 + u.cs;
+    const uint4* sl = st;
+    const uint4* sr = st + SW;
+    const int xr0 = xs - HW - (rmin + u.r0 + 31);
+    const int ri = u.r0 + lane;
     const int real = rmin + ri;
-    uint16_t* out = hs + (size_t)r * kTiX * kTiRs + ri;
+    uint16_t* out = hs + ((size_t)u.r * kTiX + u.cs) * kTiRs + ri;
     const bool store = ri < rn;
     // every window column inside the image and every right pixel too: no clamps, no range checks
-    const bool interior = x0 - HW >= 0 && x0 + kTiX - 1 + HW < W && xr0 >= 0 && xr0 + SW + 30 < W;
+    const bool interior = xs - HW >= 0 && xs + kTiSeg - 1 + HW < W && xr0 >= 0 && xr0 + SW + 30 < W;
     auto walk = [&](auto inner) {
         constexpr bool IN = decltype(inner)::value;
         const uint4* srl = sr + (31 - lane);   // right pixel of column j: srl[j] (interior)
@@ -511,7 +542,7 @@ __device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, ui
             if (IN) {
                 e = bt_pixel(sl[j], srl[j]);
             } else {
-                const int gx = iclamp(x0 - HW + j, 0, W - 1);
+                const int gx = iclamp(xs - HW + j, 0, W - 1);
                 const int x2 = gx - real;
                 e = (x2 >= 0 && x2 < W) ? bt_pixel(sl[j], sr[x2 - xr0]) : 255;
             }
@@ -529,41 +560,75 @@ __device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, ui
     };
     if (interior) walk(std::true_type{});
     else walk(std::false_type{});
-    __syncwarp();   // the staging buffer is refilled by the warp's next unit
+}
+
+// Phase 1 of one cluster: the warp's units, each unit's features copied
+// while the unit before it is walked (two staging buffers per warp).
+template <int HW>
+__device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, uint4* stg, int x0, int y0, int rmin,
+                                            int rn, int warp, int lane)
+{
+    const int nch = (rn + 31) >> 5;   // 32 real disparities per unit
+    const int per_row = 2 * nch;
+    const int units = (kTiY + 2 * HW) * per_row;
+    auto unit = [&](int k) -> BtUnit {
+        const int r = k / per_row, rem = k - r * per_row;
+        return {r, iclamp(y0 - HW + r, 0, J.h - 1), (rem & 1) * kTiSeg, (rem >> 1) * 32};
+    };
+    int k = warp;
+    if (k < units) bt_stage<HW>(J, stg, unit(k), x0, rmin, lane);
+    tile_commit();
+    for (int b = 0; k < units; k += kTiWarps, b ^= 1) {
+        const int kn = k + kTiWarps;
+        if (kn < units) bt_stage<HW>(J, stg + (b ^ 1) * kTiStage, unit(kn), x0, rmin, lane);
+        tile_commit();
+        tile_wait1();
+        __syncwarp();
+        bt_walk<HW>(J, hs, stg + b * kTiStage, unit(k), x0, rmin, rn, lane);
+        __syncwarp();   // this buffer is refilled for the unit after next
+    }
+    tile_wait0();
 }
 
 template <int NJ>
-__global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ Jobs<NJ> jobs)
+__global__ void __launch_bounds__(256, 2) k_cost_bt_tiled(const __grid_constant__ Jobs<NJ> jobs)
 {
     const LevelDesc& J = jobs.d[blockIdx.z];
     const int x0 = blockIdx.x * kTiX, y0 = blockIdx.y * kTiY;
     if (x0 >= J.w || y0 >= J.h) return;
     const int W = J.w, H = J.h, D = J.D, h = J.bs / 2;
-    extern __shared__ __align__(16) uint16_t hs[];   // [kTiY + 2h][kTiX][kTiRs], then per warp kTiStage uint4
-    uint4* stg = reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(hs) + kTiHs) + (threadIdx.x >> 5) * kTiStage;
-    __shared__ int wred[4][kTiY];
+    extern __shared__ __align__(16) uint16_t hs[];   // [kTiY + 2h][kTiX][kTiRs], then per warp 2 x kTiStage uint4
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int x = x0 + lane, y = y0 + warp;
-    const bool inside = x < W && y < H;
-    const int b = inside ? (int)J.base[(size_t)y * W + x] : (int)kNoParent;
-    const bool has = inside && b != kNoParent;
-    auto block_minmax = [&](bool in, int v, int& mn, int& mx) {
-        const int a = __reduce_min_sync(0xffffffffu, in ? v : INT_MAX);
-        const int z = __reduce_max_sync(0xffffffffu, in ? v : INT_MIN);
+    uint4* stg = reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(hs) + kTiHs) + warp * 2 * kTiStage;
+    __shared__ int wred[2][kTiWarps];
+    // a thread's two pixels: (x0 + lane, y0 + warp) and (x0 + lane, y0 + warp + 8)
+    const int x = x0 + lane;
+    int yq[2], bq[2];
+    bool inq[2], hasq[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        yq[i] = y0 + warp + 8 * i;
+        inq[i] = x < W && yq[i] < H;
+        bq[i] = inq[i] ? (int)J.base[(size_t)yq[i] * W + x] : (int)kNoParent;
+        hasq[i] = inq[i] && bq[i] != kNoParent;
+    }
+    auto block_minmax = [&](bool in0, bool in1, int& mn, int& mx) {
+        const int a = __reduce_min_sync(0xffffffffu, imin(in0 ? bq[0] : INT_MAX, in1 ? bq[1] : INT_MAX));
+        const int z = __reduce_max_sync(0xffffffffu, imax(in0 ? bq[0] : INT_MIN, in1 ? bq[1] : INT_MIN));
         __syncthreads();   // wred reused
         if (lane == 0) { wred[0][warp] = a; wred[1][warp] = z; }
         __syncthreads();
         mn = INT_MAX;
         mx = INT_MIN;
 #pragma unroll
-        for (int i = 0; i < kTiY; ++i) { mn = imin(mn, wred[0][i]); mx = imax(mx, wred[1][i]); }
+        for (int i = 0; i < kTiWarps; ++i) { mn = imin(mn, wred[0][i]); mx = imax(mx, wred[1][i]); }
     };
     // Real disparities the tile needs: [min base, max base + D - 1].  When
     // they span more than kTiRn (a depth edge through the tile), the bases
     // are split at the midpoint of their range into two clusters, each
     // handled by its own pass when it fits.
     int bmin, bmax;
-    block_minmax(has, b, bmin, bmax);
+    block_minmax(hasq[0], hasq[1], bmin, bmax);
     int ncl = 0, cut = INT_MAX;
     int cmin[2] = {bmin, 0}, cmax[2] = {bmax, 0};
     if (bmax != INT_MIN && h <= kTiMaxHalf) {
@@ -572,91 +637,98 @@ __global__ void __launch_bounds__(256) k_cost_bt_tiled(const __grid_constant__ J
         } else {
             cut = bmin + ((bmax - bmin) >> 1);
             int a0, a1, b0, b1;
-            block_minmax(has && b <= cut, b, a0, a1);
-            block_minmax(has && b > cut, b, b0, b1);
+            block_minmax(hasq[0] && bq[0] <= cut, hasq[1] && bq[1] <= cut, a0, a1);
+            block_minmax(hasq[0] && bq[0] > cut, hasq[1] && bq[1] > cut, b0, b1);
             if (a1 + D - a0 <= kTiRn && b1 + D - b0 <= kTiRn) {
                 ncl = 2;
                 cmin[0] = a0; cmax[0] = a1; cmin[1] = b0; cmax[1] = b1;
             }
         }
     }
-    int lo, hi;
-    label_range(J, x, b, lo, hi);
-    int16_t* out = J.C + ((size_t)(inside ? y : 0) * W + (inside ? x : 0)) * D;
     const bool vec = (D & 7) == 0;
     for (int c = 0; c < ncl; ++c) {
         const int rmin = cmin[c], rn = cmax[c] + D - cmin[c];
-        const int nch = (rn + 31) >> 5;   // 32 real disparities per warp pass
-        for (int u = warp; u < (kTiY + 2 * h) * nch; u += kTiY) {
-            const int r = u / nch, r0 = (u - r * nch) * 32;
-            const int gy = iclamp(y0 - h + r, 0, H - 1);
-            if (h == 2) bt_row_sums<2>(J, hs, stg, r, gy, x0, rmin, r0, rn, lane);
-            else if (h == 1) bt_row_sums<1>(J, hs, stg, r, gy, x0, rmin, r0, rn, lane);
-            else bt_row_sums<0>(J, hs, stg, r, gy, x0, rmin, r0, rn, lane);
-        }
+        if (h == 2) bt_row_sums<2>(J, hs, stg, x0, y0, rmin, rn, warp, lane);
+        else if (h == 1) bt_row_sums<1>(J, hs, stg, x0, y0, rmin, rn, warp, lane);
+        else bt_row_sums<0>(J, hs, stg, x0, y0, rmin, rn, warp, lane);
         __syncthreads();
-        if (has && (ncl == 1 || (c == 0) == (b <= cut))) {
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            if (!(hasq[i] && (ncl == 1 || (c == 0) == (bq[i] <= cut)))) continue;
+            const int ty = warp + 8 * i;
+            int lo, hi;
+            label_range(J, x, bq[i], lo, hi);
+            int16_t* out = J.C + ((size_t)yq[i] * W + x) * D;
             // packed pair sums of 2h+1 rows from offset ri0 = b - rmin (halves), 8 labels per chunk
-            const int ri0 = b - rmin;
+            const int ri0 = bq[i] - rmin;
             const uint32_t sh = (uint32_t)(ri0 & 1) * 16;
             for (int d0 = 0; d0 < D; d0 += 8) {
                 uint32_t acc[5] = {0u, 0u, 0u, 0u, 0u};
                 for (int k = 0; k <= 2 * h; ++k) {
                     const uint32_t* row =
-                        reinterpret_cast<const uint32_t*>(hs + ((warp + k) * kTiX + lane) * kTiRs) + ((ri0 + d0) >> 1);
+                        reinterpret_cast<const uint32_t*>(hs + ((ty + k) * kTiX + lane) * kTiRs) + ((ri0 + d0) >> 1);
 #pragma unroll
                     for (int j = 0; j < 5; ++j) acc[j] += row[j];
                 }
                 uint32_t w[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    w[i] = __funnelshift_r(acc[i], acc[i + 1], sh);
-                    const int d = d0 + 2 * i;
-                    if (d < lo || d > hi) w[i] = (w[i] & 0xffff0000u) | (uint32_t)kMax;
-                    if (d + 1 < lo || d + 1 > hi) w[i] = (w[i] & 0xffffu) | ((uint32_t)kMax << 16);
+                for (int q = 0; q < 4; ++q) {
+                    w[q] = __funnelshift_r(acc[q], acc[q + 1], sh);
+                    const int d = d0 + 2 * q;
+                    if (d < lo || d > hi) w[q] = (w[q] & 0xffff0000u) | (uint32_t)kMax;
+                    if (d + 1 < lo || d + 1 > hi) w[q] = (w[q] & 0xffffu) | ((uint32_t)kMax << 16);
                 }
                 if (vec) {
                     reinterpret_cast<uint4*>(out + d0)[0] = make_uint4(w[0], w[1], w[2], w[3]);
                 } else {
-                    for (int i = 0; i < 8 && d0 + i < D; ++i)
-                        out[d0 + i] = (int16_t)((w[i >> 1] >> ((i & 1) * 16)) & 0xffffu);
+                    for (int q = 0; q < 8 && d0 + q < D; ++q)
+                        out[d0 + q] = (int16_t)((w[q >> 1] >> ((q & 1) * 16)) & 0xffffu);
                 }
             }
         }
         __syncthreads();   // the next cluster's row sums overwrite hs
     }
-    if (!inside || (ncl > 0 && has)) return;
-    // direct window per pixel
-    for (int d0 = 0; d0 < D; d0 += 8) {
-        int sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (b != kNoParent) {
-            for (int dy = -h; dy <= h; ++dy) {
-                const int gy = iclamp(y + dy, 0, H - 1);
-                const uint4* lrow = J.featL + (size_t)gy * W;
-                const uint4* rrow = J.featR + (size_t)gy * W;
-                for (int dx = -h; dx <= h; ++dx) {
-                    const int gx = iclamp(x + dx, 0, W - 1);
-                    const uint4 lf = __ldg(&lrow[gx]);
+    // direct window per pixel (no parent, or not in a cluster)
+#pragma unroll 1
+    for (int i = 0; i < 2; ++i) {
+        const bool in = i ? inq[1] : inq[0], has = i ? hasq[1] : hasq[0];
+        if (!in || (ncl > 0 && has)) continue;
+        const int y = i ? yq[1] : yq[0], b = i ? bq[1] : bq[0];
+        int lo, hi;
+        label_range(J, x, b, lo, hi);
+        int16_t* out = J.C + ((size_t)y * W + x) * D;
+        for (int d0 = 0; d0 < D; d0 += 8) {
+            int sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (b != kNoParent) {
+                for (int dy = -h; dy <= h; ++dy) {
+                    const int gy = iclamp(y + dy, 0, H - 1);
+                    const uint4* lrow = J.featL + (size_t)gy * W;
+                    const uint4* rrow = J.featR + (size_t)gy * W;
+                    for (int dx = -h; dx <= h; ++dx) {
+                        const int gx = iclamp(x + dx, 0, W - 1);
+                        const uint4 lf = __ldg(&lrow[gx]);
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const int x2 = gx - (b + d0 + i);
-                        sum[i] += (x2 >= 0 && x2 < W) ? bt_pixel(lf, __ldg(&rrow[x2])) : 255;
+                        for (int q = 0; q < 8; ++q) {
+                            const int x2 = gx - (b + d0 + q);
+                            sum[q] += (x2 >= 0 && x2 < W) ? bt_pixel(lf, __ldg(&rrow[x2])) : 255;
+                        }
                     }
                 }
             }
-        }
-        uint32_t w[4];
+            uint32_t w[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int d = d0 + 2 * i;
-            const uint32_t v0 = (d >= lo && d <= hi) ? (uint32_t)imin(sum[2 * i], kMax - 1) : (uint32_t)kMax;
-            const uint32_t v1 = (d + 1 >= lo && d + 1 <= hi) ? (uint32_t)imin(sum[2 * i + 1], kMax - 1) : (uint32_t)kMax;
-            w[i] = v0 | (v1 << 16);
-        }
-        if (vec) {
-            reinterpret_cast<uint4*>(out + d0)[0] = make_uint4(w[0], w[1], w[2], w[3]);
-        } else {
-            for (int i = 0; i < 8 && d0 + i < D; ++i) out[d0 + i] = (int16_t)((w[i >> 1] >> ((i & 1) * 16)) & 0xffffu);
+            for (int q = 0; q < 4; ++q) {
+                const int d = d0 + 2 * q;
+                const uint32_t v0 = (d >= lo && d <= hi) ? (uint32_t)imin(sum[2 * q], kMax - 1) : (uint32_t)kMax;
+                const uint32_t v1 =
+                    (d + 1 >= lo && d + 1 <= hi) ? (uint32_t)imin(sum[2 * q + 1], kMax - 1) : (uint32_t)kMax;
+                w[q] = v0 | (v1 << 16);
+            }
+            if (vec) {
+                reinterpret_cast<uint4*>(out + d0)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+            } else {
+                for (int q = 0; q < 8 && d0 + q < D; ++q) out[d0 + q] = (int16_t)((w[q >> 1] >> ((q & 1) * 16)) & 0xffffu);
+            }
         }
     }
 }
