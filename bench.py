@@ -384,25 +384,32 @@ class ReferenceRunner:
 
 
 # ---------------------------------------------------------------------------
-def cpu_baseline(pairs, budget_s: float = 25.0) -> dict:
+def cpu_baseline(pairs, budget_s: float = 20.0) -> dict:
     """The oracle (CPU restatement of the reference path, OpenMP over rows /
-    columns) on host cores, on a bounded sample of the same workload."""
+    columns) on host cores, on a bounded sample of the same workload: the
+    step's pairs in order (Census and BT alternating) until `budget_s` has
+    passed, with the spread of the per-pair times."""
     import numpy as np
     from tests import _oracle
     orc = _oracle.oracle()
     cores = os.cpu_count() or 1
     orc.orc_set_num_threads(cores)
-    done, t0 = 0, time.perf_counter()
+    per = []
+    t0 = time.perf_counter()
     for left, right, c in pairs:
         p = params_for(c)
         lut = _oracle.p2_table_libm(p["p2"], 3.041, 16.137, 0.601, 1.77)
+        t = time.perf_counter()
         _oracle.orc_matcher(np.ascontiguousarray(left), np.ascontiguousarray(right), lut, **p)
-        done += 1
-        if time.perf_counter() - t0 > budget_s or done >= 2:
+        per.append(time.perf_counter() - t)
+        if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    return {"value": round(done / dt, 4), "unit": "pairs/s", "cores": orc.orc_num_threads(), "kind": "port",
-            "sample": f"{done} full 1920x1080 D=256 L3 pair(s) (Census first, then BT), adaptive P2 table from libm"}
+    s = sorted(per)
+    return {"value": round(len(per) / dt, 4), "unit": "pairs/s", "cores": orc.orc_num_threads(), "kind": "port",
+            "sample": f"{len(per)} full 1920x1080 D=256 L3 pairs (Census and BT alternating), adaptive P2 table "
+                      f"from libm; {budget_s:.0f} s budget",
+            "pair_s": {"min": round(s[0], 4), "median": round(s[len(s) // 2], 4), "max": round(s[-1], 4)}}
 
 
 def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_timing: bool) -> dict:
@@ -573,7 +580,8 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
     srv.close()
     served = {"pairs_per_s": round(st["pairs_per_s"], 2), "p50_ms": round(st["p50_ms"], 3),
               "p99_ms": round(st["p99_ms"], 3), "p999_ms": round(st["p999_ms"], 3),
-              "mean_batch": round(st["mean_batch"], 2), "completed": int(st["completed"]), "refused": refused}
+              "mean_batch": round(st["mean_batch"], 2), "completed": int(st["completed"]), "refused": refused,
+              "timeline_ms": {k: round(v, 3) for k, v in tl.items()}}
     # (b) plain sequential compute() on the same arrival stream
     dev = torch.device("cuda")
     matchers, bufs = {}, {}
@@ -776,10 +784,15 @@ def run(args) -> dict | None:
         pg.set_autotune(False)
     if args.impl == "mine" and world == 1:
         out["latency_1080p_d256_l2_census"] = single_pair_latency(dev, stream)
+    if args.impl == "mine" and world == 1:
+        out["batched_mixed"] = batched_mixed(dev, stream, flush)
     if args.impl == "mine" and world == 1 and args.serve_requests > 0:
         import pyrsgm_gb300 as pg
         rate = round(0.7 * value, 1)
         out["serving"] = serve_compare(pairs, lambda c: pg.Params(**params_for(c)), rate, args.serve_requests)
+        pool, cfg = mixed_pool(args.pool)
+        out["serving_mixed"] = [serve_compare(pool, lambda k: cfg[k], r, args.mixed_requests, seed=int(r))
+                                for r in args.mixed_rates]
     if not args.no_cpu and world == 1:
         out["cpu_baseline"] = cpu_baseline(pairs)
     return out
@@ -831,25 +844,117 @@ def single_pair_latency(dev, stream, runs: int = 20) -> dict:
 MIX_SIZES = [(640, 480), (960, 540), (1280, 720), (1920, 1080)]
 
 
-def serve_sweep(args) -> None:
-    """Serving on the mixed stream (sizes 640x480..1920x1080, D in {64,128,256},
-    pyramid levels 1-4, Census/BT): one JSON line per arrival rate."""
+def mixed_params(rng) -> dict:
+    """Parameters of one pair of the mixed workload: D from {64, 128, 256},
+    pyramid_levels 1-4, Census / BT 50/50 (each with the penalties the
+    1080p workload uses), adaptive P2 and median on."""
+    D = int(rng.choice([64, 128, 256]))
+    L = int(rng.integers(1, 5))
+    c = int(rng.integers(2))
+    return dict(num_disparities=D, pyramid_levels=L, cost_mode=c, p1=8 if c == CENSUS else 300,
+                p2=32 if c == CENSUS else 2400, adaptive_p2=True, median_filter=True, lr_check=True,
+                uniqueness_ratio=10, pyramid_coarse_disparities=128)
+
+
+def mixed_images():
+    """One seeded synthetic pair per size of the mixed workload (disparities
+    up to 255, 10 slanted patches); the pairs of the workload reuse them."""
+    from pyrsgm_gb300 import synth
+    return {s: synth.make_pair(s[0], s[1], 255, 10, 4000 + k)[:2] for k, s in enumerate(MIX_SIZES)}
+
+
+def mixed_pool(n: int, seed: int = 4000):
+    """n pairs drawn like the mixed workload: sizes 25 % each of
+    640x480 / 960x540 / 1280x720 / 1920x1080, parameters from mixed_params."""
+    import pyrsgm_gb300 as pg
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    imgs = mixed_images()
+    pool, cfg = [], []
+    for i in range(n):
+        s = MIX_SIZES[int(rng.integers(len(MIX_SIZES)))]
+        left, right = imgs[s]
+        pool.append((left, right, i))
+        cfg.append(pg.Params(**mixed_params(rng)))
+    return pool, cfg
+
+
+def batched_mixed(dev, stream, flush, npairs: int = 64, steps: int = 10) -> dict:
+    """The mixed batched workload: `npairs` pairs drawn like mixed_pool
+    (seeded; sizes, D, depth, cost per pair) in one BatchEngine run per step
+    (a CUDA graph after the first run; kernel shapes autotuned), against the
+    same pairs through per-pair StereoMatcher::compute(), both device-resident
+    with CUDA events on the compute stream and the L2 flushed between steps."""
     import numpy as np
     import torch
     import pyrsgm_gb300 as pg
-    from pyrsgm_gb300 import synth
-    torch.cuda.set_device(0)
     rng = np.random.default_rng(4000)
-    pool, cfg = [], []
-    for i in range(args.pool):
-        w, h = MIX_SIZES[rng.integers(len(MIX_SIZES))]
-        D = int(rng.choice([64, 128, 256]))
-        L = int(rng.integers(1, 5))
-        c = int(rng.integers(2))
-        left, right, _ = synth.make_pair(w, h, D - 1, 10, 4000 + i)
-        pool.append((left, right, i))
-        cfg.append(pg.Params(num_disparities=D, pyramid_levels=L, cost_mode=c, p1=8 if c else 300,
-                             p2=32 if c else 2400))
+    imgs = {s: (torch.from_numpy(l).to(dev), torch.from_numpy(r).to(dev)) for s, (l, r) in mixed_images().items()}
+    items, shapes = [], []
+    for i in range(npairs):
+        w, h = MIX_SIZES[i % 4] if i < 4 else MIX_SIZES[int(rng.integers(len(MIX_SIZES)))]
+        p = mixed_params(rng)
+        L, R = imgs[(w, h)]
+        items.append(dict(left=L, right=R, params=pg.Params(**p),
+                          disp16=torch.empty((h, w), dtype=torch.int16, device=dev),
+                          disp32=torch.empty((h, w), dtype=torch.float32, device=dev),
+                          conf=torch.empty((h, w), dtype=torch.float32, device=dev)))
+        shapes.append((w, h))
+    prev = pg.set_autotune(True)
+    eng = pg.BatchEngine(60 << 30)
+    arr = pg.BatchEngine.make_pairs(items)
+
+    def timed(fn, n):
+        ms = []
+        for _ in range(n):
+            with torch.cuda.stream(stream):
+                flush.fill_(5)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return ms
+
+    for _ in range(3):
+        eng.run_pairs(arr, True, stream)
+    torch.cuda.synchronize()
+    bms = timed(lambda: eng.run_pairs(arr, True, stream), steps)
+    pg.set_autotune(prev)
+    eng.close()
+    matchers = {}
+    for it in items:
+        key = (it["left"].shape[1], it["left"].shape[0], tuple(sorted(vars(it["params"]).items())))
+        if key not in matchers:
+            matchers[key] = pg.StereoMatcher(key[0], key[1], it["params"])
+        it["m"] = matchers[key]
+
+    def plain():
+        for it in items:
+            it["m"].compute_into(it["left"], it["right"], it["disp16"], it["disp32"], it["conf"], stream)
+
+    plain()
+    torch.cuda.synchronize()
+    pms = timed(plain, 3)
+    for m in matchers.values():
+        m.close()
+    mpix = sum(w * h for w, h in shapes) / 1e6
+    bstep, pstep = statistics.median(bms), statistics.median(pms)
+    return {"pairs_per_step": npairs, "value": round(npairs / (bstep / 1e3), 2), "unit": "pairs/s",
+            "ms_per_step": round(bstep, 4), "mpix_per_s": round(mpix / (bstep / 1e3), 1),
+            "plain_compute": {"value": round(npairs / (pstep / 1e3), 2), "ms_per_step": round(pstep, 4)},
+            "workload": "sizes 25 % each of 640x480 / 960x540 / 1280x720 / 1920x1080, D in {64,128,256}, "
+                        "pyramid_levels 1-4, Census/BT 50/50, seeded; one synthetic image pair per size",
+            "l2": "flushed (256 MB write) between steps"}
+
+
+def serve_sweep(args) -> None:
+    """Serving on the mixed stream (sizes 640x480..1920x1080, D in {64,128,256},
+    pyramid levels 1-4, Census/BT): one JSON line per arrival rate."""
+    import torch
+    torch.cuda.set_device(0)
+    pool, cfg = mixed_pool(args.pool)
     for rate in args.rates:
         res = serve_compare(pool, lambda k: cfg[k], rate, args.serve_requests, seed=int(rate),
                             max_batch=args.serve_batch, streams=args.serve_streams)
@@ -866,10 +971,13 @@ def main():
     ap.add_argument("--mode", choices=["batched", "plain", "serve"], default="batched",
                     help="headline execution: one batched run per step, or per-pair compute(); "
                          "'serve' sweeps arrival rates on the mixed-size stream")
-    ap.add_argument("--serve-requests", type=int, default=160,
+    ap.add_argument("--serve-requests", type=int, default=400,
                     help="requests of the serving comparison (0 skips it)")
+    ap.add_argument("--mixed-requests", type=int, default=1000,
+                    help="requests per rate of the mixed-stream serving comparison in the default line")
+    ap.add_argument("--mixed-rates", type=float, nargs="*", default=[1000, 4000, 16000])
     ap.add_argument("--rates", type=float, nargs="*", default=[500, 1000, 2000, 5000, 10000, 20000])
-    ap.add_argument("--pool", type=int, default=24, help="distinct pairs of the serving sweep")
+    ap.add_argument("--pool", type=int, default=24, help="distinct pairs (shapes, parameters) of the mixed stream")
     ap.add_argument("--serve-batch", type=int, default=16, help="server: largest batch")
     ap.add_argument("--serve-streams", type=int, default=2, help="server: stream lanes")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")

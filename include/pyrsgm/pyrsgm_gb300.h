@@ -168,6 +168,14 @@ int pyrsgm_gb300_server_drain(void* server, double timeout_s);
  * in host memory), mean batch size, pairs/s (first submit -> last
  * completion), peak pairs in flight, refused submissions, max latency ms. */
 int pyrsgm_gb300_server_stats(void* server, double* out10);
+/* Where a request's time goes, as means since the last reset (out8[8]):
+ * queue wait per request (submit -> batch formed), host time to enqueue a
+ * batch, GPU time of a batch (its input copies to its output copies, waits
+ * behind other lanes' work included), host time from a batch's completion to
+ * the results in the callers' buffers (all ms); then the number of batches,
+ * the longest enqueue (ms), the fraction of batches whose kernels came from a
+ * captured CUDA graph, and 0. */
+int pyrsgm_gb300_server_timeline(void* server, double* out8);
 void pyrsgm_gb300_server_reset_stats(void* server);
 /* Test hook: the next `batches` batches fail on the host before reaching the
  * GPU, as an allocation failure would; their requests report -1. */

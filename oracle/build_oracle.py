@@ -20,7 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE = "/root/reference"
+# the reference source tree (only this build step reads it); PYRSGM_REFERENCE overrides
+REFERENCE = os.environ.get("PYRSGM_REFERENCE", "/root/reference")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 ORACLE_SO = os.path.join(BUILD, "libsgm_oracle.so")

@@ -103,6 +103,7 @@ _SIGS = {
     "pyrsgm_gb300_server_drain": (_i, [_vp, C.c_double]),
     "pyrsgm_gb300_server_stats": (_i, [_vp, C.POINTER(C.c_double)]),
     "pyrsgm_gb300_server_reset_stats": (None, [_vp]),
+    "pyrsgm_gb300_server_timeline": (_i, [_vp, C.POINTER(C.c_double)]),
     "pyrsgm_gb300_server_inject_failure": (_i, [_vp, _i]),
     "pyrsgm_gb300_server_register": (_i, [_vp, _vp, _sz, C.c_char_p, _sz]),
     "pyrsgm_gb300_server_unregister": (_i, [_vp, _vp]),

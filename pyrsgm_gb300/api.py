@@ -363,6 +363,15 @@ class Server:
         lib().pyrsgm_gb300_server_stats(self._h, o)
         return dict(zip(self.STATS, list(o)))
 
+    TIMELINE = ("queue_wait_ms", "enqueue_ms", "gpu_ms", "complete_ms", "batches", "enqueue_max_ms",
+                "graph_fraction")
+
+    def timeline(self) -> dict:
+        """Mean per-stage times since the last reset (pyrsgm_gb300_server_timeline)."""
+        o = (C.c_double * 8)()
+        lib().pyrsgm_gb300_server_timeline(self._h, o)
+        return dict(zip(self.TIMELINE, list(o)))
+
     def reset_stats(self) -> None:
         lib().pyrsgm_gb300_server_reset_stats(self._h)
 

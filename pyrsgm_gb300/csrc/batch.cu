@@ -13,9 +13,10 @@
 // (width, height, validated parameters) and reused across runs; a run that
 // would exceed the engine's byte budget fails before touching the GPU.
 // CUDA graphs: a run whose signature (shapes, parameters, device pointers)
-// matches a cached one replays that graph; otherwise the run is captured,
-// instantiated and cached (a handful of signatures, least recently used
-// dropped).
+// matches a cached one replays that graph; a signature seen before but not
+// cached is captured, instantiated and cached (32 signatures, least recently
+// used dropped); a signature's first run is enqueued directly (with the
+// autotuner, that run also measures the kernel shapes of its new launches).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -148,10 +149,11 @@ public:
         }
     }
 
-    void run(const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph)
+    // True when the run's kernels came from a CUDA graph (replayed or just captured).
+    bool run(const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph)
     {
         std::lock_guard<std::mutex> lk(mu_);
-        if (n <= 0) return;
+        if (n <= 0) return false;
         std::vector<pyrsgm::Params> val(n);
         for (int i = 0; i < n; ++i) {
             const pyrsgm_gb300_pair& p = pairs[i];
@@ -170,25 +172,27 @@ public:
                     check(cudaGraphLaunch(it->exec, st), "graph launch");
                     count_launches(it->kernels);
                     it->last_use = ++tick_;
-                    return;
+                    return true;
                 }
             }
             cudaStreamCaptureStatus cs;
             check(cudaStreamIsCapturing(st, &cs), "capture status");
             if (cs != cudaStreamCaptureStatusNone) use_graph = false;  // caller is capturing: just enqueue
+            // a signature is captured the second time it comes: batches of a
+            // one-off composition (a server's mixed traffic) are enqueued
+            // directly instead of paying for a capture and an instantiation
+            if (use_graph && seen_[sig]++ == 0) {
+                if (seen_.size() > 4096) seen_.clear();
+                TuningScope scope;
+                enqueue(pairs, plans, n, st);
+                return false;
+            }
         }
         if (!use_graph) {
             // measures unknown shape keys unless the stream is being captured
             TuningScope scope;
             enqueue(pairs, plans, n, st);
-            return;
-        }
-        if (autotune_enabled()) {
-            // first run of this batch: measure the kernel shapes of its
-            // aggregation launches (outputs are complete either way), then
-            // capture with the choices recorded
-            TuningScope scope;
-            enqueue(pairs, plans, n, st);
+            return false;
         }
         cudaGraph_t g = nullptr;
         check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -215,6 +219,7 @@ public:
         const unsigned long long kernels = launch_count() - n0;
         graphs_.push_back({std::move(sig), exec, ++tick_, kernels});
         check(cudaGraphLaunch(exec, st), "graph launch");
+        return true;
     }
 
 private:
@@ -224,7 +229,7 @@ private:
         unsigned long long last_use;
         unsigned long long kernels;
     };
-    static constexpr size_t kMaxGraphs = 8;
+    static constexpr size_t kMaxGraphs = 32;
 
     // Plans for the pairs of one run: the i-th pair of a shape gets that
     // shape's i-th pooled plan (the same plans for the same batch).
@@ -355,14 +360,15 @@ private:
     size_t budget_ = 0, used_ = 0;
     std::map<ShapeKey, std::vector<std::unique_ptr<PairPlan>>> pool_;
     std::vector<Cached> graphs_;
+    std::map<std::vector<long long>, int> seen_;   // signatures run so far (uncaptured first runs)
     unsigned long long tick_ = 0;
 };
 
 BatchEngine* batch_engine_new(size_t budget) { return new BatchEngine(budget); }
 void batch_engine_delete(BatchEngine* e) { delete e; }
-void batch_engine_run(BatchEngine* e, const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph)
+bool batch_engine_run(BatchEngine* e, const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph)
 {
-    e->run(pairs, n, st, use_graph);
+    return e->run(pairs, n, st, use_graph);
 }
 void batch_engine_reserve(BatchEngine* e, int w, int h, const pyrsgm::Params& p, int count, cudaStream_t st)
 {

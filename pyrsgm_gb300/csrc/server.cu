@@ -109,12 +109,13 @@ struct IOBuf {
 class BatchEngine;
 BatchEngine* batch_engine_new(size_t budget);
 void batch_engine_delete(BatchEngine* e);
-void batch_engine_run(BatchEngine* e, const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph);
+bool batch_engine_run(BatchEngine* e, const pyrsgm_gb300_pair* pairs, int n, cudaStream_t st, bool use_graph);
 void batch_engine_reserve(BatchEngine* e, int w, int h, const pyrsgm::Params& p, int count, cudaStream_t st);
 
 struct Lane {
     cudaStream_t st = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr, done = nullptr;   // around the batch's GPU work (H2D .. D2H)
+    double t_formed = 0, t_enqueued = 0;            // host clock: batch formed, all work enqueued
     BatchEngine* eng = nullptr;
     std::map<std::pair<int, int>, std::vector<std::unique_ptr<IOBuf>>> pool;
     std::vector<Request*> reqs;
@@ -123,6 +124,7 @@ struct Lane {
     bool busy = false;       // a batch is assigned to the lane and not yet finished
     bool launched = false;   // that batch is enqueued; the lane's completion thread takes it
     std::string error;  // set when the batch failed before reaching the GPU
+    bool graph = false;  // the batch's kernels came from a captured graph
 };
 
 class Server {
@@ -135,7 +137,7 @@ public:
         for (int i = 0; i < n; ++i) {
             auto L = std::make_unique<Lane>();
             if (cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking) != cudaSuccess ||
-                cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming) != cudaSuccess)
+                cudaEventCreate(&L->start) != cudaSuccess || cudaEventCreate(&L->done) != cudaSuccess)
                 throw std::runtime_error("server: stream/event creation failed");
             L->eng = batch_engine_new(lane_budget_);
             lanes_.push_back(std::move(L));
@@ -160,6 +162,7 @@ public:
             for (auto& kv : L->pool)
                 for (auto& b : kv.second) b->release();
             batch_engine_delete(L->eng);
+            cudaEventDestroy(L->start);
             cudaEventDestroy(L->done);
             cudaStreamDestroy(L->st);
         }
@@ -252,9 +255,32 @@ public:
         o[9] = l.empty() ? 0.0 : l.back();
     }
 
+    // Mean per-stage times since the last reset: request wait in the queue,
+    // host time to enqueue a batch (copies, kernels or graph replay), GPU
+    // time of a batch (its H2D copies to its D2H copies, including time
+    // spent waiting behind the other lanes' work), host time from the
+    // batch's completion to its results in the callers' buffers; then the
+    // batch count, the longest enqueue, and the fraction of batches whose
+    // kernels came from a captured graph.
+    void timeline(double* o)
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        const double nb = tl_batches_ ? (double)tl_batches_ : 1.0;
+        o[0] = tl_reqs_ ? tl_qwait_ms_ / tl_reqs_ : 0.0;
+        o[1] = tl_enqueue_ms_ / nb;
+        o[2] = tl_gpu_ms_ / nb;
+        o[3] = tl_complete_ms_ / nb;
+        o[4] = (double)tl_batches_;
+        o[5] = tl_enqueue_max_ms_;
+        o[6] = tl_batches_ ? (double)tl_graph_ / nb : 0.0;
+        o[7] = 0.0;
+    }
+
     void reset_stats()
     {
         std::lock_guard<std::mutex> lk(mu_);
+        tl_qwait_ms_ = tl_enqueue_ms_ = tl_gpu_ms_ = tl_complete_ms_ = tl_enqueue_max_ms_ = 0;
+        tl_batches_ = tl_reqs_ = tl_graph_ = 0;
         lat_ms_.clear();
         ok_ = failed_ = refused_ = 0;
         batches_ = batched_pairs_ = 0;
@@ -392,6 +418,9 @@ private:
                     queue_.pop_front();
                 }
                 L->busy = true;
+                L->t_formed = now_s();
+                for (Request* q : batch) tl_qwait_ms_ += (L->t_formed - q->t_submit) * 1e3;
+                tl_reqs_ += (long long)batch.size();
                 inflight_ += (int)batch.size();
                 max_inflight_pairs_ = std::max(max_inflight_pairs_, (long long)inflight_);
                 ++batches_;
@@ -401,6 +430,11 @@ private:
                     fail_batch = true;
                 }
             }
+            // canonical order (by shape): the same mix of shapes gets the same
+            // buffers and plans, so the engine's graph of that mix replays
+            std::stable_sort(batch.begin(), batch.end(), [](const Request* a, const Request* b) {
+                return shape_key(a->r) < shape_key(b->r);
+            });
             L->reqs = batch;
             L->bufs.clear();
             L->staged.clear();
@@ -413,18 +447,33 @@ private:
                 cudaGetLastError();
             }
             cudaEventRecord(L->done, L->st);
+            L->t_enqueued = now_s();
             {
                 std::lock_guard<std::mutex> lk(mu_);
+                const double ms = (L->t_enqueued - L->t_formed) * 1e3;
+                tl_enqueue_ms_ += ms;
+                tl_enqueue_max_ms_ = std::max(tl_enqueue_max_ms_, ms);
                 L->launched = true;
             }
             cv_.notify_all();
         }
     }
 
+    static std::vector<long long> shape_key(const pyrsgm_gb300_request& r)
+    {
+        const pyrsgm_gb300_params& p = r.params;
+        return {r.width, r.height, p.num_disparities, p.pyramid_levels, p.cost_mode, p.min_disparity, p.block_size,
+                p.p1, p.p2, p.uniqueness_ratio, p.disp12_max_diff, p.lr_check, p.median_filter, p.num_paths,
+                p.pre_filter_cap, p.pyramid_coarse_disparities, p.pyramid_max_disparity, p.adaptive_p2,
+                (long long)(r.h_disp16 != nullptr), (long long)(r.h_disp32 != nullptr),
+                (long long)(r.h_conf != nullptr)};
+    }
+
     void launch(Lane& L)
     {
         std::map<std::pair<int, int>, int> used;
         std::vector<pyrsgm_gb300_pair> pairs;
+        cudaEventRecord(L.start, L.st);
         for (Request* q : L.reqs) {
             const pyrsgm_gb300_request& r = q->r;
             IOBuf* b = take_buf(L, r.width, r.height, used);
@@ -459,7 +508,7 @@ private:
             p.params = r.params;
             pairs.push_back(p);
         }
-        batch_engine_run(L.eng, pairs.data(), (int)pairs.size(), L.st, false);
+        L.graph = batch_engine_run(L.eng, pairs.data(), (int)pairs.size(), L.st, true);
         for (size_t i = 0; i < L.reqs.size(); ++i) {
             const pyrsgm_gb300_request& r = L.reqs[i]->r;
             IOBuf* b = L.bufs[i];
@@ -491,7 +540,13 @@ private:
                 if (!L->launched) return;
             }
             const cudaError_t e = cudaEventSynchronize(L->done);
+            const double t_gpu = now_s();
             std::string err = L->error;
+            float gpu_ms = 0.0f;
+            if (err.empty() && e == cudaSuccess && cudaEventElapsedTime(&gpu_ms, L->start, L->done) != cudaSuccess) {
+                cudaGetLastError();
+                gpu_ms = 0.0f;
+            }
             if (err.empty() && e != cudaSuccess) err = cudaGetErrorString(e);
             if (err.empty()) {
                 const cudaError_t e2 = cudaStreamQuery(L->st);
@@ -523,6 +578,12 @@ private:
                     }
                 }
                 inflight_ -= (int)L->reqs.size();
+                if (err.empty()) {
+                    ++tl_batches_;
+                    tl_gpu_ms_ += gpu_ms;
+                    tl_complete_ms_ += (t - t_gpu) * 1e3;
+                    if (L->graph) ++tl_graph_;
+                }
                 L->reqs.clear();
                 L->launched = false;
                 L->busy = false;
@@ -547,6 +608,8 @@ private:
     bool stop_ = false;
     int inject_ = 0;
     std::vector<double> lat_ms_;
+    double tl_qwait_ms_ = 0, tl_enqueue_ms_ = 0, tl_gpu_ms_ = 0, tl_complete_ms_ = 0, tl_enqueue_max_ms_ = 0;
+    long long tl_batches_ = 0, tl_reqs_ = 0, tl_graph_ = 0;
     long long ok_ = 0, failed_ = 0, refused_ = 0, batches_ = 0, batched_pairs_ = 0, max_inflight_pairs_ = 0;
     double first_submit_ = 0, last_done_ = 0;
     std::thread sched_;
@@ -604,6 +667,13 @@ int pyrsgm_gb300_server_stats(void* s, double* out10)
 {
     if (!s || !out10) return -1;
     static_cast<pg::Server*>(s)->stats(out10);
+    return 0;
+}
+
+int pyrsgm_gb300_server_timeline(void* s, double* out8)
+{
+    if (!s || !out8) return -1;
+    static_cast<pg::Server*>(s)->timeline(out8);
     return 0;
 }
 
