@@ -577,6 +577,7 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
             refused += 1
     srv.drain()
     st = srv.stats()
+    tl = srv.timeline()
     srv.close()
     served = {"pairs_per_s": round(st["pairs_per_s"], 2), "p50_ms": round(st["p50_ms"], 3),
               "p99_ms": round(st["p99_ms"], 3), "p999_ms": round(st["p999_ms"], 3),
