@@ -514,7 +514,7 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
 
 
 def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, max_batch: int = 16,
-                  streams: int = 2, budget: int = 40 << 30) -> dict:
+                  streams: int = 2, budget: int = 40 << 30, register: bool = True) -> dict:
     """n requests with Poisson arrivals at `rate` pairs/s, served (a) by the
     continuous-batching server and (b) by plain sequential compute() of one
     StereoMatcher per shape (one request at a time: H2D, compute, D2H).
@@ -539,13 +539,14 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
     srv = pg.Server(budget, max_batch=max_batch, streams=streams, max_queue=nout - max_batch * streams)
     # the caller's reused image and output arrays are page-locked once (as the
     # plain loop below uses pinned buffers)
-    for l, r, _ in pairs_pool:
-        srv.register(l)
-        srv.register(r)
-    for s_outs in outs.values():
-        for o in s_outs:
-            for a in o.values():
-                srv.register(a)
+    if register:
+        for l, r, _ in pairs_pool:
+            srv.register(l)
+            srv.register(r)
+        for s_outs in outs.values():
+            for o in s_outs:
+                for a in o.values():
+                    srv.register(a)
     # every lane keeps max_batch plans of every shape resident (a plan
     # allocated inside the timed stream would stall its lane), then every
     # pool pair runs once
