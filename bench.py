@@ -547,8 +547,8 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
             for o in s_outs:
                 for a in o.values():
                     srv.register(a)
-    # every lane keeps max_batch plans of every shape resident (a plan
-    # allocated inside the timed stream would stall its lane), then every
+    # the server's pool keeps plans of every shape resident (a plan
+    # allocated inside the timed stream would stall the lanes), then every
     # pool pair runs once
     counts = {}
     for l, _, c in pairs_pool:
@@ -556,7 +556,7 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
         counts[key] = counts.get(key, 0) + 1
     for key, cnt in counts.items():
         try:
-            srv.reserve(key[0], key[1], params_of(key[2]), min(max_batch, 2 * cnt))
+            srv.reserve(key[0], key[1], params_of(key[2]), min(max_batch, 4 * cnt))
         except RuntimeError:   # the lanes' budget is full: later shapes allocate on first use
             break
     for rep in range(2):

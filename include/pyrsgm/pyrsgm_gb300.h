@@ -150,9 +150,11 @@ typedef struct pyrsgm_gb300_request {
     pyrsgm_gb300_params params;
 } pyrsgm_gb300_request;
 
-/* num_streams lanes, each with its own stream, batch engine and
- * device_budget_bytes / num_streams of pooled device memory; batches of at
- * most max_batch pairs; at most max_queue requests waiting. */
+/* num_streams lanes, each with its own copy stream and input/output
+ * buffers; one batch engine (pooled pair plans within device_budget_bytes)
+ * whose kernels run on one compute stream shared by the lanes; batches of
+ * at most max_batch pairs and device_budget_bytes / num_streams of plans;
+ * at most max_queue requests waiting. */
 void* pyrsgm_gb300_server_create(size_t device_budget_bytes, int max_batch, int num_streams, int max_queue,
                                  char* err, size_t err_len);
 void pyrsgm_gb300_server_destroy(void* server);
@@ -186,9 +188,10 @@ int pyrsgm_gb300_server_inject_failure(void* server, int batches);
  * reason in err.  Unregister only while no request using it is in flight;
  * the server unregisters what is left when destroyed. */
 int pyrsgm_gb300_server_register(void* server, void* host, size_t bytes, char* err, size_t err_len);
-/* The same reservation on every stream lane (returns when allocated): a
- * server expecting bursts of one shape keeps that many plans per lane
- * resident, so no request waits for a device allocation. */
+/* Plans for `count` pairs of one shape kept resident in the server's pool,
+ * which all stream lanes share (returns when allocated): a server expecting
+ * bursts of one shape keeps that many plans resident, so no request waits
+ * for a device allocation. */
 int pyrsgm_gb300_server_reserve(void* server, int width, int height, const pyrsgm_gb300_params* params, int count,
                                 char* err, size_t err_len);
 int pyrsgm_gb300_server_unregister(void* server, void* host);

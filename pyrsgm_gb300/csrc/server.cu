@@ -20,10 +20,11 @@
 // page-locked with cudaHostRegister) are copied by DMA directly; other
 // buffers go through the lane's pinned staging with a host memcpy.
 //
-// Device memory stays resident: each lane keeps its batch engine's pooled
-// pair plans and a pool of input/output buffers per image size.  A request
-// is admitted only if it fits a lane's budget on its own; a batch is cut
-// where the next request would push the lane past its budget.  Failures are
+// Device memory stays resident: the lanes share one batch engine, whose
+// pooled pair plans may use the whole budget, and each lane keeps a pool of
+// input/output buffers per image size.  A request is admitted only if it
+// fits a lane's share of the budget on its own; a batch is cut where the
+// next request would push it past that share.  Failures are
 // per request (status -1 with a message): an invalid request is refused at
 // submission, a full queue refuses new requests, and a batch whose
 // allocation or launch fails fails its own requests while the server keeps
@@ -121,12 +122,12 @@ struct Lane {
     cudaEvent_t start = nullptr, done = nullptr;   // around the batch's GPU work (H2D .. D2H)
     cudaEvent_t inputs = nullptr, computed = nullptr;   // H2D finished; the batch's kernels finished
     double t_formed = 0, t_enqueued = 0;            // host clock: batch formed, all work enqueued
-    BatchEngine* eng = nullptr;
     std::map<std::pair<int, int>, std::vector<std::unique_ptr<IOBuf>>> pool;
     std::vector<Request*> reqs;
     std::vector<IOBuf*> bufs;
     std::vector<void*> staged;   // per request and output: staging used (null: copied in place or absent)
     bool busy = false;       // a batch is assigned to the lane and not yet finished
+    bool computing = false;  // that batch's kernels have not finished yet
     bool launched = false;   // that batch is enqueued; the lane's completion thread takes it
     std::string error;  // set when the batch failed before reaching the GPU
     bool graph = false;  // the batch's kernels came from a captured graph
@@ -141,6 +142,10 @@ public:
         lane_budget_ = budget / n;
         if (cudaStreamCreateWithFlags(&cst_, cudaStreamNonBlocking) != cudaSuccess)
             throw std::runtime_error("server: stream creation failed");
+        // one engine (one pool of pair plans) for all lanes: their kernels
+        // run one batch after another on the compute stream, so a plan is
+        // never used by two batches at once
+        eng_ = batch_engine_new(budget);
         for (int i = 0; i < n; ++i) {
             auto L = std::make_unique<Lane>();
             if (cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking) != cudaSuccess ||
@@ -148,7 +153,6 @@ public:
                 cudaEventCreateWithFlags(&L->inputs, cudaEventDisableTiming) != cudaSuccess ||
                 cudaEventCreateWithFlags(&L->computed, cudaEventDisableTiming) != cudaSuccess)
                 throw std::runtime_error("server: stream/event creation failed");
-            L->eng = batch_engine_new(lane_budget_);
             lanes_.push_back(std::move(L));
         }
         sched_ = std::thread([this] { schedule(); });
@@ -170,7 +174,6 @@ public:
             cudaStreamSynchronize(L->st);
             for (auto& kv : L->pool)
                 for (auto& b : kv.second) b->release();
-            batch_engine_delete(L->eng);
             cudaEventDestroy(L->start);
             cudaEventDestroy(L->done);
             cudaEventDestroy(L->inputs);
@@ -178,6 +181,7 @@ public:
             cudaStreamDestroy(L->st);
         }
         cudaStreamSynchronize(cst_);
+        batch_engine_delete(eng_);
         cudaStreamDestroy(cst_);
         for (auto& kv : reg_) cudaHostUnregister(reinterpret_cast<void*>(kv.first));
     }
@@ -315,10 +319,8 @@ public:
     {
         try {
             const pyrsgm::Params p = toParams(prm);
-            for (auto& l : lanes_) {
-                batch_engine_reserve(l->eng, w, h, p, count, cst_);
-                if (cudaStreamSynchronize(cst_) != cudaSuccess) throw std::runtime_error("reserve: stream error");
-            }
+            batch_engine_reserve(eng_, w, h, p, count, cst_);
+            if (cudaStreamSynchronize(cst_) != cudaSuccess) throw std::runtime_error("reserve: stream error");
             return 0;
         } catch (const std::exception& e) {
             err = e.what();
@@ -416,6 +418,11 @@ private:
                 cv_.wait(lk, [&] {
                     if (stop_) return true;
                     if (queue_.empty()) return false;
+                    // a batch is formed once no earlier batch is still computing:
+                    // what arrives meanwhile joins it instead of waiting behind
+                    // it in a small batch of its own
+                    for (auto& l : lanes_)
+                        if (l->computing) return false;
                     for (auto& l : lanes_)
                         if (!l->busy) return true;
                     return false;
@@ -424,6 +431,7 @@ private:
                 for (auto& l : lanes_)
                     if (!l->busy) { L = l.get(); break; }
                 if (!L) continue;
+                L->computing = true;
                 size_t bytes = 0;
                 while (!queue_.empty() && (int)batch.size() < max_batch_ && bytes + queue_.front()->bytes <= lane_budget_) {
                     bytes += queue_.front()->bytes;
@@ -527,7 +535,7 @@ private:
         // each other's kernels, never kernels with kernels)
         if (cudaEventRecord(L.inputs, L.st) != cudaSuccess || cudaStreamWaitEvent(cst_, L.inputs, 0) != cudaSuccess)
             throw std::runtime_error("input event failed");
-        L.graph = batch_engine_run(L.eng, pairs.data(), (int)pairs.size(), cst_, true);
+        L.graph = batch_engine_run(eng_, pairs.data(), (int)pairs.size(), cst_, true);
         if (cudaEventRecord(L.computed, cst_) != cudaSuccess || cudaStreamWaitEvent(L.st, L.computed, 0) != cudaSuccess)
             throw std::runtime_error("compute event failed");
         for (size_t i = 0; i < L.reqs.size(); ++i) {
@@ -560,6 +568,14 @@ private:
                 cv_.wait(lk, [&] { return L->launched || (stop_ && queue_.empty() && !L->busy); });
                 if (!L->launched) return;
             }
+            // the next batch may form as soon as this one's kernels are done
+            // (its output copies overlap the next batch's input copies)
+            if (L->error.empty()) cudaEventSynchronize(L->computed);
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                L->computing = false;
+            }
+            cv_.notify_all();
             const cudaError_t e = cudaEventSynchronize(L->done);
             const double t_gpu = now_s();
             std::string err = L->error;
@@ -616,6 +632,7 @@ private:
 
     const int max_batch_, max_queue_;
     cudaStream_t cst_ = nullptr;   // compute stream shared by the lanes
+    BatchEngine* eng_ = nullptr;   // pair plans and graphs shared by the lanes
     std::mutex reg_mu_;
     std::map<uintptr_t, size_t> reg_;   // registered host ranges: start -> bytes
     size_t lane_budget_ = 0;

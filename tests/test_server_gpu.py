@@ -151,9 +151,9 @@ def test_registered_buffers_are_copied_in_place():
 
 
 def test_reserved_plans_serve_bursts_without_allocation():
-    """Plans reserved up front on every lane: a burst of that shape runs on
-    them and gives the results of each pair alone; a reservation beyond a
-    lane's budget is refused."""
+    """Plans reserved up front in the server's pool (shared by its lanes): a
+    burst of that shape runs on them and gives the results of each pair
+    alone; a reservation beyond the server's budget is refused."""
     p = pg.Params(num_disparities=64, pyramid_levels=1, cost_mode=pg.COST_CENSUS, p1=8, p2=32)
     w, h = 160, 96
     one = pg.pair_bytes(w, h, p)
@@ -167,7 +167,7 @@ def test_reserved_plans_serve_bursts_without_allocation():
         np.testing.assert_array_equal(out["disp16"], want["disp16"])
         np.testing.assert_allclose(out["conf"], want["conf"], rtol=0, atol=1e-6)
     with pytest.raises(RuntimeError, match="budget"):
-        srv.reserve(w, h, p, 40)   # 40 plans per lane > a lane's 32-plan budget
+        srv.reserve(w, h, p, 65)   # 65 plans > the 64-plan budget
     srv.close()
 
 
