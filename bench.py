@@ -559,12 +559,19 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
             srv.reserve(key[0], key[1], params_of(key[2]), min(max_batch, 4 * cnt))
         except RuntimeError:   # the lanes' budget is full: later shapes allocate on first use
             break
-    for rep in range(2):
+    # warm-up: the pool in bursts for at least a second (every shape's
+    # kernels loaded, the GPU out of its idle clocks)
+    t_w = time.perf_counter()
+    while True:
         ids = [srv.submit(l, r, params_of(c), outputs=outs[(l.shape[1], l.shape[0])][k % nout])[0]
-               for k, (l, r, c) in enumerate(pairs_pool)]
+               for k, (l, r, c) in enumerate(pairs_pool[:max_batch * streams])]
         for rid in ids:
             srv.wait(rid)
+        if time.perf_counter() - t_w > 1.0:
+            break
     srv.reset_stats()
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.__enter__()
     refused = 0
     t0 = time.perf_counter()
     for i in range(n):
@@ -577,13 +584,14 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
         except ValueError:
             refused += 1
     srv.drain()
+    clk.__exit__(None, None, None)
     st = srv.stats()
     tl = srv.timeline()
     srv.close()
     served = {"pairs_per_s": round(st["pairs_per_s"], 2), "p50_ms": round(st["p50_ms"], 3),
               "p99_ms": round(st["p99_ms"], 3), "p999_ms": round(st["p999_ms"], 3),
               "mean_batch": round(st["mean_batch"], 2), "completed": int(st["completed"]), "refused": refused,
-              "timeline_ms": {k: round(v, 3) for k, v in tl.items()}}
+              "timeline_ms": {k: round(v, 3) for k, v in tl.items()}, "clocks": clk.summary()}
     # (b) plain sequential compute() on the same arrival stream
     dev = torch.device("cuda")
     matchers, bufs = {}, {}
