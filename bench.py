@@ -54,9 +54,12 @@ def params_for(cost: int) -> dict:
 
 
 # Measured DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of
-# the aggregation launches per algorithmic byte, filled in from the committed
-# capture of the aggregation kernels (None: no capture of this build yet).
-AGG_TRAFFIC_PER_ALG_BYTE = None
+# the aggregation launches per byte they move by their own design, from the
+# full capture of the level-0 launches of four 1080p pairs
+# (profiles/stage_kernels_1080p_4pairs.md): k_gtb 513 + k_grow 1037 + k_wta
+# 914 MB against 556 + 1112 + 912 MB of their own bytes.  Scaled to a step
+# by those bytes (every kernel streams its volumes once per launch).
+AGG_TRAFFIC_PER_ALG_BYTE = 2464.0 / 2580.0
 
 
 def alg_bytes(width: int, height: int, params: dict) -> dict:

@@ -34,6 +34,7 @@
 #include "pyrsgm/pyrsgm_c.h"
 #include "pyrsgm/pyrsgm_gb300.h"
 #include "sgm_launch.h"
+#include "trace.h"
 
 namespace pyrsgm {
 Params validateParams(const Params& in);
@@ -297,6 +298,7 @@ private:
 
     void enqueue(const pyrsgm_gb300_pair* pairs, const std::vector<PairPlan*>& plans, int n, cudaStream_t st)
     {
+        TraceRange tr("pyrsgm.batch %d pairs", n);
         int maxL = 0;
         for (int i = 0; i < n; ++i) maxL = std::max(maxL, plans[i]->levels);
         // pyramids, one level of every pair per launch group
@@ -337,6 +339,7 @@ private:
                 jobs.push_back({d, level});
             }
             if (jobs.empty()) continue;
+            TraceRange tround("pyrsgm.round %d (%d level jobs)", r, (int)jobs.size());
             auto all = [](const LevelDesc&) { return 0; };
             launchGrouped(jobs, all, [](const Jobs<kBatchJobs>& b, const LevelExtent& e, cudaStream_t s) {
                 return launch_prepare(b, e, s);

@@ -22,6 +22,7 @@
 #include "pyrsgm/pyrsgm_gb300.h"
 #include "sgm_launch.h"
 #include "workspace.h"
+#include "trace.h"
 
 namespace pg {
 
@@ -191,6 +192,7 @@ void fill_workspace_ptrs(LevelDesc& d, const Workspace& ws)
 int run_level_single(const LevelDesc& d, cudaStream_t st, float alpha, float beta, float lower, float upper,
                      const char* what)
 {
+    TraceRange tr("pyrsgm.%s (%dx%d, %d labels)", what, d.w, d.h, d.D);
     Jobs<1> j;
     j.d[0] = d;
     j.n = 1;

@@ -48,6 +48,7 @@
 #include <vector>
 
 #include "pair_plan.h"
+#include "trace.h"
 #include "pyrsgm/pyrsgm_gb300.h"
 
 namespace pyrsgm {
@@ -68,6 +69,7 @@ struct Request {
     size_t bytes = 0;
     double t_submit = 0, t_done = 0;
     int status = 0;  // 0 pending, 1 done, -1 failed
+    unsigned long long trace = 0;   // NVTX range submit -> completion
     std::string error;
 };
 
@@ -215,6 +217,7 @@ public:
         }
         q->id = next_id_++;
         q->t_submit = now_s();
+        q->trace = trace_start("pyrsgm.request");
         if (first_submit_ == 0) first_submit_ = q->t_submit;
         Request* raw = q.get();
         all_[raw->id] = std::move(q);
@@ -492,6 +495,7 @@ private:
 
     void launch(Lane& L)
     {
+        TraceRange tr("pyrsgm.server.batch %d pairs", (int)L.reqs.size());
         std::map<std::pair<int, int>, int> used;
         std::vector<pyrsgm_gb300_pair> pairs;
         cudaEventRecord(L.start, L.st);
@@ -603,6 +607,7 @@ private:
                 std::lock_guard<std::mutex> lk(mu_);
                 for (Request* q : L->reqs) {
                     q->t_done = t;
+                    trace_end(q->trace);
                     if (err.empty()) {
                         q->status = 1;
                         ++ok_;

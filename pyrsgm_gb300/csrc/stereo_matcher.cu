@@ -20,6 +20,7 @@
 #include "pyrsgm/pyrsgm_c.h"
 #include "pyrsgm/pyrsgm_gb300.h"
 #include "pair_plan.h"
+#include "trace.h"
 #include "sgm_launch.h"
 #include "workspace.h"
 
@@ -139,6 +140,7 @@ struct StereoMatcher::Impl {
         if (!L || !R) throw std::invalid_argument("pyrsgm: null input image");
         if (!d16 && !d32 && !c) return;
         if (d16 && (d16p % 2) != 0) throw std::invalid_argument("pyrsgm: disp16 pitch must be even");
+        pg::TraceRange tr("pyrsgm.compute %dx%d L%d", plan.width, plan.height, plan.levels);
         // both views of a pyramid level in one launch
         for (int level = 1; level <= plan.levels; ++level) {
             pg::PyrDownBatch<2> b;
@@ -150,6 +152,7 @@ struct StereoMatcher::Impl {
         for (int level = plan.levels; level >= 0; --level) {
             const pg::LevelDesc d =
                 level == 0 ? plan.level0(L, lp, R, rp, d16, d16p, d32, d32p, c, cp) : plan.levelDesc(level);
+            pg::TraceRange tl("pyrsgm.level %d (%dx%d, %d labels)", level, d.w, d.h, d.D);
             runLevel(d, level, st);
         }
     }
