@@ -455,13 +455,16 @@ __global__ void __launch_bounds__(256) k_cost_bt_box(const __grid_constant__ Job
 // through the window and the real disparity, so one 32x16 tile evaluates
 // each (window pixel, real disparity) pair once when the real disparities
 // its pixels need, [min base, max base + D - 1], span at most kTiRn:
-//   phase 1: units of (window row, half row of 16 output columns, 32 real
-//            disparities) are dealt to the 8 warps in turn; a warp walks
-//            its unit's columns left to right, one real disparity per
-//            lane, keeping the running sum of the last blockSize costs
-//            (sums along x, into shared memory).  The features of a
-//            warp's next unit are copied with cp.async while it walks the
-//            current one;
+//   staging: the features of every window row of the tile (left: one per
+//            window column, clamped; right: the ones its disparities reach)
+//            are copied once into shared memory with cp.async;
+//   phase 1: the (window row, real disparity) pairs of a half row of 16
+//            output columns are numbered row-major and cut into units of
+//            32, one pair per lane, dealt to the 8 warps in turn; a lane
+//            walks its half row left to right and keeps the running sum of
+//            the last blockSize costs (sums along x, into shared memory).
+//            A tile usually needs 17 real disparities, so numbering the
+//            pairs this way keeps nearly every lane busy;
 //   phase 2: a thread per pixel adds blockSize rows of those sums, two
 //            labels per 32-bit add, from its own real-disparity offset.
 // Window sums are exact integers (at most 25 * 255 here, no intermediate
@@ -469,13 +472,15 @@ __global__ void __launch_bounds__(256) k_cost_bt_box(const __grid_constant__ Job
 // split into two base clusters (a pass each); pixels in neither, or a
 // wider window, evaluate each window directly.
 // ---------------------------------------------------------------------------
-constexpr int kTiX = 32, kTiY = 16, kTiRn = 64, kTiMaxHalf = 2;
+constexpr int kTiX = 32, kTiY = 16, kTiRn = 32, kTiMaxHalf = 2;
 constexpr int kTiWarps = 8;
-constexpr int kTiSeg = 16;                  // output columns of a row-sum unit
-constexpr int kTiRs = kTiRn + 2;   // halves per (row, column): 33 words, odd, so columns hit distinct banks
-constexpr int kTiStage = 2 * (kTiSeg + 2 * kTiMaxHalf) + 31;   // staged left (SW) + right (SW + 31) features of a unit
-constexpr size_t kTiHs = (size_t)(kTiY + 2 * kTiMaxHalf) * kTiX * kTiRs * 2;
-constexpr size_t kTiSmem = kTiHs + (size_t)kTiWarps * 2 * kTiStage * 16;
+constexpr int kTiSeg = 16;                          // output columns of a half row
+constexpr int kTiRows = kTiY + 2 * kTiMaxHalf;      // window rows at most
+constexpr int kTiRs = kTiRn + 2;   // halves per (row, column): 17 words, odd, so columns hit distinct banks
+constexpr int kTiSL = kTiX + 2 * kTiMaxHalf;        // staged left features per window row
+constexpr int kTiSR = kTiSL + kTiRn - 1;            // staged right features per window row
+constexpr size_t kTiHs = (size_t)kTiRows * kTiX * kTiRs * 2;
+constexpr size_t kTiSmem = kTiHs + (size_t)kTiRows * (kTiSL + kTiSR) * 16;
 
 __device__ __forceinline__ void tile_cp16(void* dst, const void* src)
 {
@@ -483,111 +488,84 @@ __device__ __forceinline__ void tile_cp16(void* dst, const void* src)
                  "l"(src)
                  : "memory");
 }
-__device__ __forceinline__ void tile_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void tile_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void tile_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-// A row-sum unit: window row r (image row gy), output columns x0 + cs ..
-// x0 + cs + 15, real disparities rmin + r0 .. rmin + r0 + 31.
-struct BtUnit {
-    int r, gy, cs, r0;
-};
-
-// Copy the unit's left features (one per window column, clamped) and the
-// right features its lanes reach (inside the image only) into `st`.
-template <int HW>
-__device__ __forceinline__ void bt_stage(const LevelDesc& J, uint4* st, const BtUnit& u, int x0, int rmin, int lane)
+__device__ __forceinline__ void tile_commit_wait()
 {
-    constexpr int SW = kTiSeg + 2 * HW;
-    const int W = J.w;
-    const int xs = x0 + u.cs;
-    const uint4* lrow = J.featL + (size_t)u.gy * W;
-    const uint4* rrow = J.featR + (size_t)u.gy * W;
-    const int xr0 = xs - HW - (rmin + u.r0 + 31);
-    for (int i = lane; i < SW; i += 32) tile_cp16(st + i, lrow + iclamp(xs - HW + i, 0, W - 1));
-    for (int i = lane; i < SW + 31; i += 32) {
-        const int xx = xr0 + i;
-        if (xx >= 0 && xx < W) tile_cp16(st + SW + i, rrow + xx);
-    }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
-// Sums along x of one unit for its 32 real disparities: a running sum over
-// the last 2*HW+1 costs, from the staged features.
+// Sums along x, for a cluster of real disparities rmin .. rmin + rn - 1,
+// of every window row of the tile (see above).
 template <int HW>
-__device__ __forceinline__ void bt_walk(const LevelDesc& J, uint16_t* hs, const uint4* st, const BtUnit& u, int x0,
-                                        int rmin, int rn, int lane)
-{
-    constexpr int SW = kTiSeg + 2 * HW;
-    const int W = J.w;
-    const int xs = x0 + u.cs;
-    const uint4* sl = st;
-    const uint4* sr = st + SW;
-    const int xr0 = xs - HW - (rmin + u.r0 + 31);
-    const int ri = u.r0 + lane;
-    const int real = rmin + ri;
-    uint16_t* out = hs + ((size_t)u.r * kTiX + u.cs) * kTiRs + ri;
-    const bool store = ri < rn;
-    // every window column inside the image and every right pixel too: no clamps, no range checks
-    const bool interior = xs - HW >= 0 && xs + kTiSeg - 1 + HW < W && xr0 >= 0 && xr0 + SW + 30 < W;
-    auto walk = [&](auto inner) {
-        constexpr bool IN = decltype(inner)::value;
-        const uint4* srl = sr + (31 - lane);   // right pixel of column j: srl[j] (interior)
-        int q[2 * HW + 1];                     // q[0 .. 2HW-1]: the last 2HW costs, oldest first
-#pragma unroll
-        for (int i = 0; i < 2 * HW + 1; ++i) q[i] = 0;
-        int s = 0;
-#pragma unroll
-        for (int j = 0; j < SW; ++j) {
-            int e;
-            if (IN) {
-                e = bt_pixel(sl[j], srl[j]);
-            } else {
-                const int gx = iclamp(xs - HW + j, 0, W - 1);
-                const int x2 = gx - real;
-                e = (x2 >= 0 && x2 < W) ? bt_pixel(sl[j], sr[x2 - xr0]) : 255;
-            }
-            s += e;
-            if (j >= 2 * HW && store) out[(j - 2 * HW) * kTiRs] = (uint16_t)s;
-            if (HW > 0) {
-                s -= q[0];
-#pragma unroll
-                for (int i = 0; i + 1 < 2 * HW; ++i) q[i] = q[i + 1];
-                q[2 * HW - 1 < 0 ? 0 : 2 * HW - 1] = e;
-            } else {
-                s = 0;
-            }
-        }
-    };
-    if (interior) walk(std::true_type{});
-    else walk(std::false_type{});
-}
-
-// Phase 1 of one cluster: the warp's units, each unit's features copied
-// while the unit before it is walked (two staging buffers per warp).
-template <int HW>
-__device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, uint4* stg, int x0, int y0, int rmin,
+__device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, uint4* st, int x0, int y0, int rmin,
                                             int rn, int warp, int lane)
 {
-    const int nch = (rn + 31) >> 5;   // 32 real disparities per unit
-    const int per_row = 2 * nch;
-    const int units = (kTiY + 2 * HW) * per_row;
-    auto unit = [&](int k) -> BtUnit {
-        const int r = k / per_row, rem = k - r * per_row;
-        return {r, iclamp(y0 - HW + r, 0, J.h - 1), (rem & 1) * kTiSeg, (rem >> 1) * 32};
-    };
-    int k = warp;
-    if (k < units) bt_stage<HW>(J, stg, unit(k), x0, rmin, lane);
-    tile_commit();
-    for (int b = 0; k < units; k += kTiWarps, b ^= 1) {
-        const int kn = k + kTiWarps;
-        if (kn < units) bt_stage<HW>(J, stg + (b ^ 1) * kTiStage, unit(kn), x0, rmin, lane);
-        tile_commit();
-        tile_wait1();
-        __syncwarp();
-        bt_walk<HW>(J, hs, stg + b * kTiStage, unit(k), x0, rmin, rn, lane);
-        __syncwarp();   // this buffer is refilled for the unit after next
+    constexpr int R = kTiY + 2 * HW;     // window rows
+    constexpr int SW = kTiSeg + 2 * HW;  // window columns of a half row
+    const int W = J.w, H = J.h;
+    uint4* sl = st;                      // [R][kTiSL]  left, columns x0 - HW + j (clamped)
+    uint4* sr = st + kTiRows * kTiSL;    // [R][kTiSR]  right, columns xrs + k (inside the image only)
+    const int xrs = x0 - HW - (rmin + rn - 1);
+    const int nsl = kTiX + 2 * HW, nsr = nsl + rn - 1;
+    // staging (the block's threads, one pass of copies)
+    for (int i = threadIdx.x; i < R * nsl; i += blockDim.x) {
+        const int r = i / nsl, j = i - r * nsl;
+        const int gy = iclamp(y0 - HW + r, 0, H - 1);
+        tile_cp16(sl + r * kTiSL + j, J.featL + (size_t)gy * W + iclamp(x0 - HW + j, 0, W - 1));
     }
-    tile_wait0();
+    for (int i = threadIdx.x; i < R * nsr; i += blockDim.x) {
+        const int r = i / nsr, k = i - r * nsr;
+        const int gy = iclamp(y0 - HW + r, 0, H - 1);
+        const int xx = xrs + k;
+        if (xx >= 0 && xx < W) tile_cp16(sr + r * kTiSR + k, J.featR + (size_t)gy * W + xx);
+    }
+    tile_commit_wait();
+    __syncthreads();
+    // every window column of the tile inside the image, and every right pixel too
+    const bool interior = x0 - HW >= 0 && x0 + kTiX - 1 + HW < W && xrs >= 0 && xrs + nsr - 1 < W;
+    const int pairs = R * rn;                      // (window row, real disparity) pairs of a half row
+    const int chunks = (pairs + 31) >> 5;
+    for (int u = warp; u < 2 * chunks; u += kTiWarps) {
+        const int seg = u & 1, f = (u >> 1) * 32 + lane;
+        const bool on = f < pairs;
+        const int fr = on ? f : pairs - 1;
+        const int row = fr / rn, ri = fr - row * rn;
+        const int real = rmin + ri;
+        const int c0 = seg * kTiSeg;               // first window column of the half row (tile-relative)
+        const uint4* lrow = sl + row * kTiSL + c0;
+        const uint4* rrow = sr + row * kTiSR;
+        uint16_t* out = hs + ((size_t)row * kTiX + c0) * kTiRs + ri;
+        auto walk = [&](auto inner) {
+            constexpr bool IN = decltype(inner)::value;
+            const uint4* srl = rrow + c0 - ri + rn - 1;   // right feature of window column j: srl[j] (interior)
+            int q[2 * HW + 1];
+#pragma unroll
+            for (int i = 0; i < 2 * HW + 1; ++i) q[i] = 0;
+            int s = 0;
+#pragma unroll
+            for (int j = 0; j < SW; ++j) {
+                int e;
+                if (IN) {
+                    e = bt_pixel(lrow[j], srl[j]);
+                } else {
+                    const int gx = iclamp(x0 - HW + c0 + j, 0, W - 1);
+                    const int x2 = gx - real;
+                    e = (x2 >= 0 && x2 < W) ? bt_pixel(lrow[j], rrow[x2 - xrs]) : 255;
+                }
+                s += e;
+                if (j >= 2 * HW && on) out[(j - 2 * HW) * kTiRs] = (uint16_t)s;
+                if (HW > 0) {
+                    s -= q[0];
+#pragma unroll
+                    for (int i = 0; i + 1 < 2 * HW; ++i) q[i] = q[i + 1];
+                    q[2 * HW - 1 < 0 ? 0 : 2 * HW - 1] = e;
+                } else {
+                    s = 0;
+                }
+            }
+        };
+        if (interior) walk(std::true_type{});
+        else walk(std::false_type{});
+    }
 }
 
 template <int NJ>
@@ -597,9 +575,9 @@ __global__ void __launch_bounds__(256, 2) k_cost_bt_tiled(const __grid_constant_
     const int x0 = blockIdx.x * kTiX, y0 = blockIdx.y * kTiY;
     if (x0 >= J.w || y0 >= J.h) return;
     const int W = J.w, H = J.h, D = J.D, h = J.bs / 2;
-    extern __shared__ __align__(16) uint16_t hs[];   // [kTiY + 2h][kTiX][kTiRs], then per warp 2 x kTiStage uint4
+    extern __shared__ __align__(16) uint16_t hs[];   // [kTiRows][kTiX][kTiRs], then the staged features
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint4* stg = reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(hs) + kTiHs) + warp * 2 * kTiStage;
+    uint4* stg = reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(hs) + kTiHs);
     __shared__ int wred[2][kTiWarps];
     // a thread's two pixels: (x0 + lane, y0 + warp) and (x0 + lane, y0 + warp + 8)
     const int x = x0 + lane;
