@@ -569,7 +569,7 @@ __device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, ui
 }
 
 template <int NJ>
-__global__ void __launch_bounds__(256, 2) k_cost_bt_tiled(const __grid_constant__ Jobs<NJ> jobs)
+__global__ void __launch_bounds__(256, 3) k_cost_bt_tiled(const __grid_constant__ Jobs<NJ> jobs)
 {
     const LevelDesc& J = jobs.d[blockIdx.z];
     const int x0 = blockIdx.x * kTiX, y0 = blockIdx.y * kTiY;
