@@ -112,11 +112,12 @@ struct Grp {
     static constexpr int LENW = PADW + D + 2;   // words a shifted window can touch
     static constexpr int BUFW = LENW * CPW;     // one window buffer of a warp
     static constexpr int NBUF = T == 1 ? 1 : 2;
-    // Ring slot of a thread: its NW cost words, at a stride that puts the
-    // 16- or 8-byte lane accesses of a warp in distinct banks.  The
-    // label-base and image words of a slot sit in a separate [slot][2][32]
-    // array (bank = lane).
-    static constexpr int RSW_TB = NW == 8 ? 12 : NW;
+    // Ring slot of a thread: its NW cost words.  For NW = 8 the two 16-byte
+    // halves of a slot are swapped in lanes 4-7 of every 8 (ring_half), so
+    // that the 16-byte accesses of 8 lanes at a 32-byte stride hit distinct
+    // banks.  The label-base and image words of a slot sit in a separate
+    // [slot][2][32] array (bank = lane).
+    static constexpr int RSW_TB = NW;
 };
 
 template <int NW>
@@ -172,6 +173,9 @@ __device__ __forceinline__ void cpw(uint32_t* dst, const int16_t* src)
         for (int i = 0; i < NW / 4; ++i) cp16(dst + 4 * i, src + 8 * i);
     }
 }
+
+// Position of half h (0, 1) of an NW = 8 ring slot in lane `lane`'s slot.
+__device__ __forceinline__ int ring_half(int h, int lane) { return 4 * (h ^ ((lane >> 2) & 1)); }
 
 // Minimum over the chain's words: a tree in the thread, then over the group.
 template <int NW, int T>
@@ -325,21 +329,23 @@ __device__ __forceinline__ void wta_out(const LevelDesc& J, int y, int x, int ba
 // bandwidth of line requests.  SC chunk slots in flight per warp.
 template <int D>
 __host__ __device__ constexpr int chunk_steps() { return D >= 64 ? 1 : 64 / D; }
-// Chunk slots per warp (SC - 1 runs in flight): for 4-step runs 3 measured
-// fastest on the 16-pair 1080p row pass (2: too little look-ahead; 4: the
-// larger footprint was slower as well); shorter runs keep about 6-8 steps
-// of look-ahead.
+// Chunk slots per warp (SC - 1 runs in flight): 2 for 4-step runs, which
+// with the path costs written back into the consumed slot keeps a 4-warp
+// block at 55 KB of shared memory -- 16 warps per SM, so the level-0 row
+// pass of a 32-pair 1080p batch (2160 warps) runs in one wave on 152 SMs;
+// shorter runs keep about 6-8 steps of look-ahead.
 template <int D>
-__host__ __device__ constexpr int chunk_stages() { return chunk_steps<D>() == 4 ? 3 : chunk_steps<D>() == 2 ? 4 : 6; }
+__host__ __device__ constexpr int chunk_stages() { return chunk_steps<D>() == 4 ? 2 : chunk_steps<D>() == 2 ? 4 : 6; }
 
 template <int NW, int T>
 constexpr size_t row_smem()
 {
     using G = Grp<NW, T>;
     constexpr int CH = chunk_steps<G::D>(), SC = chunk_stages<G::D>();
-    // per warp: window buffers, SC input chunk slots and one output chunk
-    // (32 words per chain each), the label-base / image ring
-    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + (SC + 1) * G::CPW * 32 + SC * CH * 64);
+    // per warp: window buffers, SC chunk slots (32 words per chain each;
+    // a step's path costs replace its costs in the slot), the label-base /
+    // image ring
+    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + SC * G::CPW * 32 + SC * CH * 64);
 }
 template <int NW, int T>
 constexpr size_t row_lane_smem()
@@ -403,7 +409,12 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_gtb(const __grid_co
     auto issue_next = [&](int slot) {
         if (yi < H) {
             uint32_t* d = ring + slot * 32 * RS;
-            cpw<NW>(d, Cg + oi);
+            if constexpr (NW == 8) {
+                cp16(d + ring_half(0, lane), Cg + oi);
+                cp16(d + ring_half(1, lane), Cg + oi + 8);
+            } else {
+                cpw<NW>(d, Cg + oi);
+            }
             if (use_base) cp4(bi + slot * 64, word_of(Bg + pi));
             if (adaptive) cp4(bi + slot * 64 + 32, word_of(Lg + li));
         }
@@ -427,7 +438,14 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_gtb(const __grid_co
         const uint32_t* db = bi + slot * 64;
         slot = slot + 1 == S ? 0 : slot + 1;
         uint32_t cc[NW];
-        ldw<NW>(d, cc);
+        if constexpr (NW == 8) {
+            const uint4 a = *reinterpret_cast<const uint4*>(d + ring_half(0, lane));
+            const uint4 b = *reinterpret_cast<const uint4*>(d + ring_half(1, lane));
+            cc[0] = a.x; cc[1] = a.y; cc[2] = a.z; cc[3] = a.w;
+            cc[4] = b.x; cc[5] = b.y; cc[6] = b.z; cc[7] = b.w;
+        } else {
+            ldw<NW>(d, cc);
+        }
         const int base = use_base ? (int)(int16_t)(db[0] >> ((pc & 1) * 16)) : J.minD;
         int p2 = J.P2;
         if (adaptive) {
@@ -474,7 +492,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
     int* lut = reinterpret_cast<int*>(smem);
     uint32_t* cbuf = smem + 256;
     uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
-    uint32_t* bibuf = rbuf + kWarps * (SC + 1) * SLOTW;
+    uint32_t* bibuf = rbuf + kWarps * SC * SLOTW;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
     for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
     __syncthreads();
@@ -486,8 +504,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
     const int yy = imin(y, J.h - 1);
     const int W = J.w, H = J.h;
     uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
-    uint32_t* ring = rbuf + warp * (SC + 1) * SLOTW;
-    uint32_t* ob = ring + SC * SLOTW;
+    uint32_t* ring = rbuf + warp * SC * SLOTW;
     uint32_t* bi = bibuf + warp * SC * CH * 64 + lane;   // [slot][2 * CH words][lane]
 
     // path extents (single-scale: kernel_AggregateLR/RL ranges)
@@ -570,7 +587,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
         islot = islot + 1 == SC ? 0 : islot + 1;
         cp_wait<SC - 1>();
         __syncwarp();
-        const uint32_t* cin = ring + slot * SLOTW;
+        uint32_t* cin = ring + slot * SLOTW;   // the chunk's costs in, its path costs out
         const uint32_t* db = bi + slot * CH * 64;
         const int t0 = ci * CH, xlo = dir ? xs - t0 - (CH - 1) : xs + t0;
         const bool full = CH == 4 && t0 + CH - 1 < n_mine;
@@ -612,12 +629,13 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
                 mask_labels<NW>(cc, lo, hi, k);
             }
             gstep<NW, T, PYR>(st, cc, base, p2, p12, chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0), k);
+            // this step's costs were read above: its path costs take their place
             if constexpr (NW == 2) {
-                *reinterpret_cast<uint2*>(ob + piece_col(c, w0 >> 2) + (w0 & 3)) = make_uint2(st.L[0], st.L[1]);
+                *reinterpret_cast<uint2*>(cin + piece_col(c, w0 >> 2) + (w0 & 3)) = make_uint2(st.L[0], st.L[1]);
             } else {
 #pragma unroll
                 for (int i = 0; i < NW / 4; ++i)
-                    *reinterpret_cast<uint4*>(ob + piece_col(c, (w0 >> 2) + i)) =
+                    *reinterpret_cast<uint4*>(cin + piece_col(c, (w0 >> 2) + i)) =
                         make_uint4(st.L[4 * i], st.L[4 * i + 1], st.L[4 * i + 2], st.L[4 * i + 3]);
             }
         }
@@ -630,7 +648,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
                 for (int j = 0; j < NCOP; ++j)
                     if (crow + 2 * j < H)
                         *reinterpret_cast<uint4*>(Og + dst + j * rstride) =
-                            *reinterpret_cast<const uint4*>(ob + piece_col(4 * j + (lane >> 3), pce));
+                            *reinterpret_cast<const uint4*>(cin + piece_col(4 * j + (lane >> 3), pce));
             }
         }
         __syncwarp();
