@@ -329,13 +329,13 @@ __device__ __forceinline__ void wta_out(const LevelDesc& J, int y, int x, int ba
 // bandwidth of line requests.  SC chunk slots in flight per warp.
 template <int D>
 __host__ __device__ constexpr int chunk_steps() { return D >= 64 ? 1 : 64 / D; }
-// Chunk slots per warp (SC - 1 runs in flight): 2 for 4-step runs, which
-// with the path costs written back into the consumed slot keeps a 4-warp
-// block at 55 KB of shared memory -- 16 warps per SM, so the level-0 row
-// pass of a 32-pair 1080p batch (2160 warps) runs in one wave on 152 SMs;
-// shorter runs keep about 6-8 steps of look-ahead.
+// Chunk slots per warp (SC - 1 runs in flight): 3 for 4-step runs; with
+// the path costs written back into the consumed slot a 4-warp block takes
+// 74 KB of shared memory, 12 warps per SM (2 slots, 16 warps per SM, was
+// slower: one run of look-ahead per warp is too little); shorter runs keep
+// about 6-8 steps of look-ahead.
 template <int D>
-__host__ __device__ constexpr int chunk_stages() { return chunk_steps<D>() == 4 ? 2 : chunk_steps<D>() == 2 ? 4 : 6; }
+__host__ __device__ constexpr int chunk_stages() { return chunk_steps<D>() == 4 ? 3 : chunk_steps<D>() == 2 ? 4 : 6; }
 
 template <int NW, int T>
 constexpr size_t row_smem()
