@@ -329,11 +329,12 @@ __device__ __forceinline__ void wta_out(const LevelDesc& J, int y, int x, int ba
 // bandwidth of line requests.  SC chunk slots in flight per warp.
 template <int D>
 __host__ __device__ constexpr int chunk_steps() { return D >= 64 ? 1 : 64 / D; }
-// Chunk slots per warp (SC - 1 runs in flight): 3 for 4-step runs; with
-// the path costs written back into the consumed slot a 4-warp block takes
-// 74 KB of shared memory, 12 warps per SM (2 slots, 16 warps per SM, was
-// slower: one run of look-ahead per warp is too little); shorter runs keep
-// about 6-8 steps of look-ahead.
+// Chunk slots per warp (SC - 1 runs in flight): for 4-step runs 3 measured
+// fastest on the 1080p row pass (2: too little look-ahead; 4: the larger
+// footprint was slower as well); shorter runs keep about 6-8 steps of
+// look-ahead.  A separate output chunk per warp (8 warps per SM) measured
+// faster than writing the path costs back into the consumed slot with 12
+// or 16 warps per SM (2.81 against 3.73 / 3.57 ms per 32-pair step).
 template <int D>
 __host__ __device__ constexpr int chunk_stages() { return chunk_steps<D>() == 4 ? 3 : chunk_steps<D>() == 2 ? 4 : 6; }
 
@@ -342,10 +343,9 @@ constexpr size_t row_smem()
 {
     using G = Grp<NW, T>;
     constexpr int CH = chunk_steps<G::D>(), SC = chunk_stages<G::D>();
-    // per warp: window buffers, SC chunk slots (32 words per chain each;
-    // a step's path costs replace its costs in the slot), the label-base /
-    // image ring
-    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + SC * G::CPW * 32 + SC * CH * 64);
+    // per warp: window buffers, SC input chunk slots and one output chunk
+    // (32 words per chain each), the label-base / image ring
+    return 256 * 4 + (size_t)warps_of<NW>() * 4 * (G::NBUF * G::BUFW + (SC + 1) * G::CPW * 32 + SC * CH * 64);
 }
 template <int NW, int T>
 constexpr size_t row_lane_smem()
@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
     int* lut = reinterpret_cast<int*>(smem);
     uint32_t* cbuf = smem + 256;
     uint32_t* rbuf = cbuf + kWarps * G::NBUF * G::BUFW;
-    uint32_t* bibuf = rbuf + kWarps * SC * SLOTW;
+    uint32_t* bibuf = rbuf + kWarps * (SC + 1) * SLOTW;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
     for (int i = threadIdx.x; i < kWarps * G::NBUF * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
     __syncthreads();
@@ -504,7 +504,8 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
     const int yy = imin(y, J.h - 1);
     const int W = J.w, H = J.h;
     uint32_t* chain = cbuf + warp * G::NBUF * G::BUFW + c;
-    uint32_t* ring = rbuf + warp * SC * SLOTW;
+    uint32_t* ring = rbuf + warp * (SC + 1) * SLOTW;
+    uint32_t* ob = ring + SC * SLOTW;
     uint32_t* bi = bibuf + warp * SC * CH * 64 + lane;   // [slot][2 * CH words][lane]
 
     // path extents (single-scale: kernel_AggregateLR/RL ranges)
@@ -587,7 +588,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
         islot = islot + 1 == SC ? 0 : islot + 1;
         cp_wait<SC - 1>();
         __syncwarp();
-        uint32_t* cin = ring + slot * SLOTW;   // the chunk's costs in, its path costs out
+        const uint32_t* cin = ring + slot * SLOTW;
         const uint32_t* db = bi + slot * CH * 64;
         const int t0 = ci * CH, xlo = dir ? xs - t0 - (CH - 1) : xs + t0;
         const bool full = CH == 4 && t0 + CH - 1 < n_mine;
@@ -629,13 +630,12 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
                 mask_labels<NW>(cc, lo, hi, k);
             }
             gstep<NW, T, PYR>(st, cc, base, p2, p12, chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0), k);
-            // this step's costs were read above: its path costs take their place
             if constexpr (NW == 2) {
-                *reinterpret_cast<uint2*>(cin + piece_col(c, w0 >> 2) + (w0 & 3)) = make_uint2(st.L[0], st.L[1]);
+                *reinterpret_cast<uint2*>(ob + piece_col(c, w0 >> 2) + (w0 & 3)) = make_uint2(st.L[0], st.L[1]);
             } else {
 #pragma unroll
                 for (int i = 0; i < NW / 4; ++i)
-                    *reinterpret_cast<uint4*>(cin + piece_col(c, (w0 >> 2) + i)) =
+                    *reinterpret_cast<uint4*>(ob + piece_col(c, (w0 >> 2) + i)) =
                         make_uint4(st.L[4 * i], st.L[4 * i + 1], st.L[4 * i + 2], st.L[4 * i + 3]);
             }
         }
@@ -648,7 +648,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
                 for (int j = 0; j < NCOP; ++j)
                     if (crow + 2 * j < H)
                         *reinterpret_cast<uint4*>(Og + dst + j * rstride) =
-                            *reinterpret_cast<const uint4*>(cin + piece_col(4 * j + (lane >> 3), pce));
+                            *reinterpret_cast<const uint4*>(ob + piece_col(4 * j + (lane >> 3), pce));
             }
         }
         __syncwarp();
