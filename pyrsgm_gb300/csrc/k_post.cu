@@ -69,36 +69,61 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
     // src/sgm_kernels.cu:825-889).
     const bool check = uses_packed(J.D) && (J.post & POST_LRCHECK);
     const bool med = (J.post & POST_MEDIAN) != 0;
-    auto disp_at = [&](int xx, int yy) -> int {
-        const int d16 = J.disp_raw[(size_t)yy * W + xx];
-        if (!check || d16 == inv) return d16;
-        const unsigned* krow = J.keys + (size_t)yy * W;
-        auto disp2 = [&](int rx) -> int {
-            const unsigned k = __ldg(krow + rx);
-            return k == 0xffffffffu ? (int)inv : (int)(0xffffu - (k & 0xffffu)) - rx;
-        };
-        const int d0 = d16 >> 4, d1 = (d16 + 15) >> 4;
-        const int r0 = xx - d0, r1 = xx - d1;
-        if (J.pyr) {
-            bool ok = false;
-            if (r0 >= 0 && r0 < W) { const int v = disp2(r0); if (v >= J.minD && abs(v - d0) <= J.maxdiff) ok = true; }
-            if (!ok && r1 != r0 && r1 >= 0 && r1 < W) {
-                const int v = disp2(r1);
-                if (v >= J.minD && abs(v - d1) <= J.maxdiff) ok = true;
-            }
-            return ok ? d16 : (int)inv;
-        }
-        bool bad0 = false, bad1 = false;
-        if (r0 >= 0 && r0 < W) { const int v = disp2(r0); bad0 = v >= J.minD && abs(v - d0) > J.maxdiff; }
-        if (r1 >= 0 && r1 < W) { const int v = disp2(r1); bad1 = v >= J.minD && abs(v - d1) > J.maxdiff; }
-        return (bad0 && bad1) ? (int)inv : d16;
-    };
+    // The LR-checked disparities of the tile and its halo, staged in three
+    // rounds so that each thread's loads are in flight together: its raw
+    // disparities, then the disp2 keys they point at, then the decisions.
     __shared__ int16_t td[kPoY + 2][kPoX + 2];   // row r, column c: pixel (y0 - 1 + r, x0 - 1 + c)
     if (check || med) {
-        for (int i = threadIdx.x; i < (kPoY + 2) * (kPoX + 2); i += blockDim.x) {
+        constexpr int kN = (kPoY + 2) * (kPoX + 2), kPer = (kN + 255) / 256;
+        int dv[kPer], xs[kPer], rowp[kPer];   // (a level has far fewer than 2^31 pixels)
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int i = threadIdx.x + 256 * k;
             const int r = i / (kPoX + 2), c = i - r * (kPoX + 2);
             const int yy = y0 - 1 + r, xx = x0 - 1 + c;
-            td[r][c] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? (int16_t)disp_at(xx, yy) : inv;
+            const bool in = i < kN && yy >= 0 && yy < H && xx >= 0 && xx < W;
+            rowp[k] = in ? yy * W : 0;
+            xs[k] = in ? xx : -1;
+            dv[k] = in ? (int)J.disp_raw[(size_t)rowp[k] + xx] : (int)inv;
+        }
+        if (check) {
+            unsigned k0[kPer], k1[kPer];
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                k0[k] = k1[k] = 0xffffffffu;
+                if (xs[k] >= 0 && dv[k] != inv) {
+                    const int r0 = xs[k] - (dv[k] >> 4), r1 = xs[k] - ((dv[k] + 15) >> 4);
+                    if (r0 >= 0 && r0 < W) k0[k] = __ldg(J.keys + (size_t)rowp[k] + r0);
+                    if (r1 >= 0 && r1 < W) k1[k] = __ldg(J.keys + (size_t)rowp[k] + r1);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int d16 = dv[k], xx = xs[k];
+                if (xx < 0 || d16 == inv) continue;
+                const int d0 = d16 >> 4, d1 = (d16 + 15) >> 4;
+                const int r0 = xx - d0, r1 = xx - d1;
+                // disp2 of right pixel rx from its key (cost << 16 | 0xffff - x)
+                auto disp2 = [&](unsigned key, int rx) -> int {
+                    return key == 0xffffffffu ? (int)inv : (int)(0xffffu - (key & 0xffffu)) - rx;
+                };
+                const bool in0 = r0 >= 0 && r0 < W, in1 = r1 >= 0 && r1 < W;
+                const int v0 = in0 ? disp2(k0[k], r0) : 0, v1 = in1 ? disp2(k1[k], r1) : 0;
+                if (J.pyr) {
+                    const bool ok = (in0 && v0 >= J.minD && abs(v0 - d0) <= J.maxdiff) ||
+                                    (in1 && v1 >= J.minD && abs(v1 - d1) <= J.maxdiff);
+                    dv[k] = ok ? d16 : (int)inv;
+                } else {
+                    const bool bad0 = in0 && v0 >= J.minD && abs(v0 - d0) > J.maxdiff;
+                    const bool bad1 = in1 && v1 >= J.minD && abs(v1 - d1) > J.maxdiff;
+                    dv[k] = (bad0 && bad1) ? (int)inv : d16;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int i = threadIdx.x + 256 * k;
+            if (i < kN) (&td[0][0])[i] = (int16_t)dv[k];
         }
         __syncthreads();
     }
