@@ -517,7 +517,7 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
 
 
 def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, max_batch: int = 16,
-                  streams: int = 2, budget: int = 40 << 30, register: bool = True) -> dict:
+                  streams: int = 2, budget: int = 40 << 30) -> dict:
     """n requests with Poisson arrivals at `rate` pairs/s, served (a) by the
     continuous-batching server and (b) by plain sequential compute() of one
     StereoMatcher per shape (one request at a time: H2D, compute, D2H).
@@ -530,9 +530,14 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
     picks = rng.integers(0, len(pairs_pool), n)
     nout = max_batch * streams + 64
 
+    def pinned(shape, dtype):
+        # page-locked host memory (cudaHostAlloc through torch), as the plain
+        # baseline below uses: copied by DMA in place by the server
+        return torch.empty(shape, dtype=dtype).pin_memory().numpy()
+
     def outputs_for(w, h):
-        return [{"disp16": np.empty((h, w), np.int16), "disp32": np.empty((h, w), np.float32),
-                 "conf": np.empty((h, w), np.float32)} for _ in range(nout)]
+        return [{"disp16": pinned((h, w), torch.int16), "disp32": pinned((h, w), torch.float32),
+                 "conf": pinned((h, w), torch.float32)} for _ in range(nout)]
 
     shapes = {}
     for l, _, c in pairs_pool:
@@ -542,14 +547,14 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
     srv = pg.Server(budget, max_batch=max_batch, streams=streams, max_queue=nout - max_batch * streams)
     # the caller's reused image and output arrays are page-locked once (as the
     # plain loop below uses pinned buffers)
-    if register:
-        for l, r, _ in pairs_pool:
-            srv.register(l)
-            srv.register(r)
-        for s_outs in outs.values():
-            for o in s_outs:
-                for a in o.values():
-                    srv.register(a)
+    # the pool's images in page-locked memory too
+    host_pool = []
+    for l, r, c in pairs_pool:
+        pl, pr = pinned(l.shape, torch.uint8), pinned(r.shape, torch.uint8)
+        pl[...] = l
+        pr[...] = r
+        host_pool.append((pl, pr, c))
+    pairs_pool = host_pool
     # the server's pool keeps plans of every shape resident (a plan
     # allocated inside the timed stream would stall the lanes), then every
     # pool pair runs once

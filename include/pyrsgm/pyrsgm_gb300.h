@@ -170,21 +170,24 @@ int pyrsgm_gb300_server_drain(void* server, double timeout_s);
  * in host memory), mean batch size, pairs/s (first submit -> last
  * completion), peak pairs in flight, refused submissions, max latency ms. */
 int pyrsgm_gb300_server_stats(void* server, double* out10);
-/* Where a request's time goes, as means since the last reset (out8[8]):
+/* Where a request's time goes, as means since the last reset (out10[10]):
  * queue wait per request (submit -> batch formed), host time to enqueue a
  * batch, GPU time of a batch (its input copies to its output copies, waits
  * behind other lanes' work included), host time from a batch's completion to
  * the results in the callers' buffers (all ms); then the number of batches,
  * the longest enqueue (ms), the fraction of batches whose kernels came from a
- * captured CUDA graph, and 0. */
-int pyrsgm_gb300_server_timeline(void* server, double* out8);
+ * captured CUDA graph, and the batch's GPU time split into input copies,
+ * kernels (with the wait for the shared compute stream) and output copies
+ * (ms). */
+int pyrsgm_gb300_server_timeline(void* server, double* out10);
 void pyrsgm_gb300_server_reset_stats(void* server);
 /* Test hook: the next `batches` batches fail on the host before reaching the
  * GPU, as an allocation failure would; their requests report -1. */
 int pyrsgm_gb300_server_inject_failure(void* server, int batches);
 /* Page-lock a host range (cudaHostRegister): request images and outputs
- * that lie inside a registered range are copied by DMA in place, the others
- * through the server's pinned staging with a host memcpy.  0, or -1 with the
+ * that lie inside a registered range -- or in memory the caller page-locked
+ * itself (cudaHostAlloc, cudaHostRegister) -- are copied by DMA in place,
+ * the others through the server's pinned staging with a host memcpy.  0, or -1 with the
  * reason in err.  Unregister only while no request using it is in flight;
  * the server unregisters what is left when destroyed. */
 int pyrsgm_gb300_server_register(void* server, void* host, size_t bytes, char* err, size_t err_len);

@@ -364,11 +364,11 @@ class Server:
         return dict(zip(self.STATS, list(o)))
 
     TIMELINE = ("queue_wait_ms", "enqueue_ms", "gpu_ms", "complete_ms", "batches", "enqueue_max_ms",
-                "graph_fraction")
+                "graph_fraction", "inputs_ms", "kernels_ms", "outputs_ms")
 
     def timeline(self) -> dict:
         """Mean per-stage times since the last reset (pyrsgm_gb300_server_timeline)."""
-        o = (C.c_double * 8)()
+        o = (C.c_double * 10)()
         lib().pyrsgm_gb300_server_timeline(self._h, o)
         return dict(zip(self.TIMELINE, list(o)))
 

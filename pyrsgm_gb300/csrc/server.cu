@@ -152,8 +152,7 @@ public:
             auto L = std::make_unique<Lane>();
             if (cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking) != cudaSuccess ||
                 cudaEventCreate(&L->start) != cudaSuccess || cudaEventCreate(&L->done) != cudaSuccess ||
-                cudaEventCreateWithFlags(&L->inputs, cudaEventDisableTiming) != cudaSuccess ||
-                cudaEventCreateWithFlags(&L->computed, cudaEventDisableTiming) != cudaSuccess)
+                cudaEventCreate(&L->inputs) != cudaSuccess || cudaEventCreate(&L->computed) != cudaSuccess)
                 throw std::runtime_error("server: stream/event creation failed");
             lanes_.push_back(std::move(L));
         }
@@ -280,8 +279,10 @@ public:
     // time of a batch (its H2D copies to its D2H copies, including time
     // spent waiting behind the other lanes' work), host time from the
     // batch's completion to its results in the callers' buffers; then the
-    // batch count, the longest enqueue, and the fraction of batches whose
-    // kernels came from a captured graph.
+    // batch count, the longest enqueue, the fraction of batches whose
+    // kernels came from a captured graph, and the GPU time split into the
+    // input copies, the kernels (with the wait for the compute stream) and
+    // the output copies.
     void timeline(double* o)
     {
         std::lock_guard<std::mutex> lk(mu_);
@@ -293,13 +294,16 @@ public:
         o[4] = (double)tl_batches_;
         o[5] = tl_enqueue_max_ms_;
         o[6] = tl_batches_ ? (double)tl_graph_ / nb : 0.0;
-        o[7] = 0.0;
+        o[7] = tl_in_ms_ / nb;
+        o[8] = tl_comp_ms_ / nb;
+        o[9] = (tl_gpu_ms_ - tl_in_ms_ - tl_comp_ms_) / nb;
     }
 
     void reset_stats()
     {
         std::lock_guard<std::mutex> lk(mu_);
         tl_qwait_ms_ = tl_enqueue_ms_ = tl_gpu_ms_ = tl_complete_ms_ = tl_enqueue_max_ms_ = 0;
+        tl_in_ms_ = tl_comp_ms_ = 0;
         tl_batches_ = tl_reqs_ = tl_graph_ = 0;
         lat_ms_.clear();
         ok_ = failed_ = refused_ = 0;
@@ -388,14 +392,30 @@ private:
         return p;
     }
 
+    // Whether a host range can be copied by DMA in place: registered with
+    // this server, or page-locked by the caller (cudaHostAlloc /
+    // cudaHostRegister elsewhere; its start and end both page-locked host
+    // memory of the same allocation).
     bool registered(const void* p, size_t bytes)
     {
         const uintptr_t a = reinterpret_cast<uintptr_t>(p);
-        std::lock_guard<std::mutex> lk(reg_mu_);
-        auto it = reg_.upper_bound(a);
-        if (it == reg_.begin()) return false;
-        --it;
-        return a >= it->first && a + bytes <= it->first + it->second;
+        {
+            std::lock_guard<std::mutex> lk(reg_mu_);
+            auto it = reg_.upper_bound(a);
+            if (it != reg_.begin()) {
+                --it;
+                if (a >= it->first && a + bytes <= it->first + it->second) return true;
+            }
+        }
+        cudaPointerAttributes at{}, bt{};
+        if (cudaPointerGetAttributes(&at, p) != cudaSuccess ||
+            cudaPointerGetAttributes(&bt, static_cast<const unsigned char*>(p) + bytes - 1) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return at.type == cudaMemoryTypeHost && bt.type == cudaMemoryTypeHost && at.hostPointer && bt.hostPointer &&
+               static_cast<const unsigned char*>(bt.hostPointer) - static_cast<const unsigned char*>(at.hostPointer) ==
+                   (ptrdiff_t)(bytes - 1);
     }
 
     IOBuf* take_buf(Lane& L, int w, int h, std::map<std::pair<int, int>, int>& used)
@@ -583,10 +603,13 @@ private:
             const cudaError_t e = cudaEventSynchronize(L->done);
             const double t_gpu = now_s();
             std::string err = L->error;
-            float gpu_ms = 0.0f;
-            if (err.empty() && e == cudaSuccess && cudaEventElapsedTime(&gpu_ms, L->start, L->done) != cudaSuccess) {
+            float gpu_ms = 0.0f, in_ms = 0.0f, comp_ms = 0.0f;
+            if (err.empty() && e == cudaSuccess &&
+                (cudaEventElapsedTime(&gpu_ms, L->start, L->done) != cudaSuccess ||
+                 cudaEventElapsedTime(&in_ms, L->start, L->inputs) != cudaSuccess ||
+                 cudaEventElapsedTime(&comp_ms, L->inputs, L->computed) != cudaSuccess)) {
                 cudaGetLastError();
-                gpu_ms = 0.0f;
+                gpu_ms = in_ms = comp_ms = 0.0f;
             }
             if (err.empty() && e != cudaSuccess) err = cudaGetErrorString(e);
             if (err.empty()) {
@@ -623,6 +646,8 @@ private:
                 if (err.empty()) {
                     ++tl_batches_;
                     tl_gpu_ms_ += gpu_ms;
+                    tl_in_ms_ += in_ms;
+                    tl_comp_ms_ += comp_ms;
                     tl_complete_ms_ += (t - t_gpu) * 1e3;
                     if (L->graph) ++tl_graph_;
                 }
@@ -653,6 +678,7 @@ private:
     int inject_ = 0;
     std::vector<double> lat_ms_;
     double tl_qwait_ms_ = 0, tl_enqueue_ms_ = 0, tl_gpu_ms_ = 0, tl_complete_ms_ = 0, tl_enqueue_max_ms_ = 0;
+    double tl_in_ms_ = 0, tl_comp_ms_ = 0;
     long long tl_batches_ = 0, tl_reqs_ = 0, tl_graph_ = 0;
     long long ok_ = 0, failed_ = 0, refused_ = 0, batches_ = 0, batched_pairs_ = 0, max_inflight_pairs_ = 0;
     double first_submit_ = 0, last_done_ = 0;
@@ -714,10 +740,10 @@ int pyrsgm_gb300_server_stats(void* s, double* out10)
     return 0;
 }
 
-int pyrsgm_gb300_server_timeline(void* s, double* out8)
+int pyrsgm_gb300_server_timeline(void* s, double* out10)
 {
-    if (!s || !out8) return -1;
-    static_cast<pg::Server*>(s)->timeline(out8);
+    if (!s || !out10) return -1;
+    static_cast<pg::Server*>(s)->timeline(out10);
     return 0;
 }
 
