@@ -517,7 +517,7 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
 
 
 def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, max_batch: int = 16,
-                  streams: int = 2, budget: int = 40 << 30) -> dict:
+                  streams: int = 2, budget: int = 40 << 30, queue: int = 16) -> dict:
     """n requests with Poisson arrivals at `rate` pairs/s, served (a) by the
     continuous-batching server and (b) by plain sequential compute() of one
     StereoMatcher per shape (one request at a time: H2D, compute, D2H).
@@ -528,7 +528,7 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
     picks = rng.integers(0, len(pairs_pool), n)
-    nout = max_batch * streams + 64
+    nout = max_batch * streams + queue   # output buffers: every request that can be waiting or in flight
 
     def pinned(shape, dtype):
         # page-locked host memory (cudaHostAlloc through torch), as the plain
@@ -572,7 +572,7 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
     t_w = time.perf_counter()
     while True:
         ids = [srv.submit(l, r, params_of(c), outputs=outs[(l.shape[1], l.shape[0])][k % nout])[0]
-               for k, (l, r, c) in enumerate(pairs_pool[:max_batch * streams])]
+               for k, (l, r, c) in enumerate(pairs_pool[:min(max_batch * streams, queue)])]
         for rid in ids:
             srv.wait(rid)
         if time.perf_counter() - t_w > 1.0:
@@ -806,8 +806,10 @@ def run(args) -> dict | None:
         out["batched_mixed"] = batched_mixed(dev, stream, flush)
     if args.impl == "mine" and world == 1 and args.serve_requests > 0:
         import pyrsgm_gb300 as pg
-        rate = round(0.7 * value, 1)
-        out["serving"] = serve_compare(pairs, lambda c: pg.Params(**params_for(c)), rate, args.serve_requests)
+        # below and above the server's capacity (its outputs' copies to host
+        # memory bound it); plain compute is overloaded at both
+        out["serving"] = [serve_compare(pairs, lambda c: pg.Params(**params_for(c)), round(f * value, 1),
+                                        args.serve_requests) for f in (0.35, 0.7)]
         pool, cfg = mixed_pool(args.pool)
         out["serving_mixed"] = [serve_compare(pool, lambda k: cfg[k], r, args.mixed_requests, seed=int(r))
                                 for r in args.mixed_rates]
