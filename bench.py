@@ -969,6 +969,49 @@ def batched_mixed(dev, stream, flush, npairs: int = 64, steps: int = 10) -> dict
             "l2": "flushed (256 MB write) between steps"}
 
 
+def stage_times(args) -> None:
+    """One batch-engine run of --batch 1080p D=256 L3 pairs (Census and BT
+    alternating, the headline workload), without a graph, after --warmup
+    runs: prints the per-stage CUDA-event times of the library profiler as
+    one JSON line.  --packed-words forces a shape of the 16/32/64-label
+    aggregation (0 = chosen per launch), --fused the fused two-pass form.
+    This is the run the per-kernel ncu summaries capture."""
+    import torch
+    import pyrsgm_gb300 as pg
+    from pyrsgm_gb300._native import lib
+    torch.cuda.set_device(0)
+    pg.set_packed_words(args.packed_words)
+    pg.set_fused(args.fused)
+    pg.set_autotune(False)
+    items = []
+    for left, right, c in make_inputs(args.batch):
+        items.append(dict(left=torch.from_numpy(left).cuda(), right=torch.from_numpy(right).cuda(),
+                          params=pg.Params(**params_for(c)),
+                          disp16=torch.empty((H, W), dtype=torch.int16, device="cuda"),
+                          disp32=torch.empty((H, W), dtype=torch.float32, device="cuda"),
+                          conf=torch.empty((H, W), dtype=torch.float32, device="cuda")))
+    eng = pg.BatchEngine(40 << 30)
+    st = torch.cuda.Stream()
+    for _ in range(args.warmup):
+        eng.run(items, use_graph=False, stream=st)
+    torch.cuda.synchronize()
+    lib().pyrsgm_gb300_profile(1)
+    eng.run(items, use_graph=False, stream=st)
+    torch.cuda.synchronize()
+    out = {}
+    for k, nm in enumerate(PROF_NAMES):
+        ms, cnt, by = C.c_double(), C.c_longlong(), C.c_double()
+        lib().pyrsgm_gb300_profile_read(k, C.byref(ms), C.byref(cnt), C.byref(by))
+        if cnt.value:
+            out[nm] = {"ms": round(ms.value, 4), "launches": cnt.value,
+                       "gbs": round(by.value / ms.value / 1e6, 1) if ms.value else 0.0}
+    lib().pyrsgm_gb300_profile(0)
+    eng.close()
+    print(json.dumps({"mode": "stages", "pairs": args.batch, "packed_words": args.packed_words,
+                      "fused": bool(args.fused), "stages": out,
+                      "total_ms": round(sum(v["ms"] for v in out.values()), 4)}), flush=True)
+
+
 def serve_sweep(args) -> None:
     """Serving on the mixed stream (sizes 640x480..1920x1080, D in {64,128,256},
     pyramid levels 1-4, Census/BT): one JSON line per arrival rate."""
@@ -988,9 +1031,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=32, help="pairs per step")
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--mode", choices=["batched", "plain", "serve"], default="batched",
+    ap.add_argument("--mode", choices=["batched", "plain", "serve", "stages"], default="batched",
                     help="headline execution: one batched run per step, or per-pair compute(); "
-                         "'serve' sweeps arrival rates on the mixed-size stream")
+                         "'serve' sweeps arrival rates on the mixed-size stream; "
+                         "'stages' prints the per-stage times of one batched run")
+    ap.add_argument("--packed-words", type=int, default=0,
+                    help="stages: 16/32/64-label aggregation shape (0 = per launch, 8, 4 or 2)")
+    ap.add_argument("--fused", action="store_true", help="stages: fused two-pass 16-label aggregation")
     ap.add_argument("--serve-requests", type=int, default=400,
                     help="requests of the serving comparison (0 skips it)")
     ap.add_argument("--mixed-requests", type=int, default=1000,
@@ -1006,6 +1053,9 @@ def main():
         args.warmup = 3
     if args.mode == "serve":
         serve_sweep(args)
+        return
+    if args.mode == "stages":
+        stage_times(args)
         return
     out = run(args)
     if out is not None:
