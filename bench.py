@@ -666,11 +666,11 @@ def job_rate(world: int, units_per_rank: float, max_ms: float) -> float:
 
 
 # profiled stages of the aggregation and the kernels behind them
-AGG_STAGES = ("path_tb", "path_row", "wta", "tblr", "rlw")
+AGG_STAGES = ("path_tb", "path_row", "wta", "tblr", "rlw", "tbw")
 AGG_KERNELS = {"path_tb": "k_gtb/k_path_tb", "path_row": "k_grow/k_path_row", "wta": "k_wta",
-               "tblr": "k_tblr", "rlw": "k_rlw"}
+               "tblr": "k_tblr", "rlw": "k_rlw", "tbw": "k_gtbw"}
 PROF_NAMES = ["pyrdown", "features", "labels", "cost", "path_tb", "path_row", "post", "p2table", "wta", "tblr",
-              "rlw"]
+              "rlw", "tbw"]
 
 
 def stage_bandwidth(prof: dict, peak_gbs: float) -> dict:

@@ -238,6 +238,15 @@ int pyrsgm_gb300_set_packed_words(int words);
  * pass; results are identical.  Returns the previous setting. */
 int pyrsgm_gb300_set_fused(int on);
 
+/* Winner-take-all inside the top-to-bottom pass for the 16-label pyramid
+ * levels with three paths, in the one-thread-per-16-labels shape (on by
+ * default; PYRSGM_GB300_TBW=0 turns it off at load).  When on, the row pass
+ * runs first and the top-to-bottom chains add their costs to the row
+ * paths' and pick the winners, instead of writing a top-to-bottom volume
+ * for a separate winner-take-all pass; results are identical.  Returns the
+ * previous setting. */
+int pyrsgm_gb300_set_tbw(int on);
+
 /* Waits of the fused pass that ran out of time (a band whose band above
  * never published its edge; results of that launch are wrong), counted on
  * the current device since load or the last reset.  Synchronous.
@@ -256,7 +265,8 @@ unsigned pyrsgm_gb300_fused_stalls(int reset);
 int pyrsgm_gb300_set_autotune(int on);
 
 typedef struct {
-    int num_labels, pyramid, rows, width;  /* key */
+    int num_labels, pyramid, rows, width;  /* key; pyramid: 0 single-scale, 1 pyramid level,
+                                              2 with the fused passes, 3 with the T->B winner-take-all */
     int words;                             /* chosen words per thread (8, or 2/4) */
     float ms_wide, ms_spread;              /* best time of each shape */
 } pyrsgm_gb300_tune_entry;
@@ -272,7 +282,8 @@ void pyrsgm_gb300_autotune_clear(void);
  * pyrsgm_gb300_profile(0) stops.  _read() waits for the recorded events of
  * one kernel kind (0 pyrDown, 1 features, 2 refine labels, 3 cost volume,
  * 4 top->bottom path, 5 row pass, 6 post, 7 P2 table, 8 winner-take-all of
- * the 16/32/64-label levels) and returns the summed
+ * the 16/32/64-label levels, 9 and 10 the fused passes, 11 top->bottom with
+ * the winner-take-all) and returns the summed
  * device time in ms, the launch count and the summed algorithmic bytes. */
 int pyrsgm_gb300_profile(int enable);
 int pyrsgm_gb300_profile_read(int kind, double* ms_total, long long* launches, double* bytes_total);

@@ -113,6 +113,7 @@ _SIGS = {
     "pyrsgm_gb300_set_packed_words": (_i, [_i]),
     "pyrsgm_gb300_set_autotune": (_i, [_i]),
     "pyrsgm_gb300_set_fused": (_i, [_i]),
+    "pyrsgm_gb300_set_tbw": (_i, [_i]),
     "pyrsgm_gb300_fused_stalls": (C.c_uint, [_i]),
     "pyrsgm_gb300_autotune_entries": (_i, [_vp, _i]),
     "pyrsgm_gb300_autotune_clear": (None, []),

@@ -219,6 +219,12 @@ def set_fused(on: bool) -> bool:
     return bool(lib().pyrsgm_gb300_set_fused(1 if on else 0))
 
 
+def set_tbw(on: bool) -> bool:
+    """Winner-take-all inside the top-to-bottom pass of the 16-label pyramid
+    levels (pyrsgm_gb300_set_tbw, on by default); returns the previous setting."""
+    return bool(lib().pyrsgm_gb300_set_tbw(1 if on else 0))
+
+
 def fused_stalls(reset: bool = False) -> int:
     """Waits of the fused pass that ran out of time (pyrsgm_gb300_fused_stalls)."""
     return int(lib().pyrsgm_gb300_fused_stalls(1 if reset else 0))

@@ -277,11 +277,14 @@ private:
         return out;
     }
 
-    // Graph key: every field of every pair (pointers, pitches, shape, parameters).
+    // Graph key: every field of every pair (pointers, pitches, shape,
+    // parameters) and the kernel-form switches, so that a switch changed
+    // after a capture takes effect on the next run.
     static std::vector<long long> signature(const pyrsgm_gb300_pair* pairs, const std::vector<pyrsgm::Params>& val,
                                             int n)
     {
         std::vector<long long> s;
+        s.push_back(packed_words_override() * 100 + fused_mode() * 10 + tbw_mode());
         for (int i = 0; i < n; ++i) {
             const pyrsgm_gb300_pair& p = pairs[i];
             const long long f[] = {(long long)(uintptr_t)p.d_left, (long long)p.left_pitch,

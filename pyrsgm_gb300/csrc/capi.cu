@@ -49,6 +49,12 @@ static std::atomic<int> g_fused{[] {
 }()};
 int fused_mode() { return g_fused.load(std::memory_order_relaxed); }
 
+static std::atomic<int> g_tbw{[] {
+    const char* e = std::getenv("PYRSGM_GB300_TBW");
+    return e && std::atoi(e) == 0 ? 0 : 1;
+}()};
+int tbw_mode() { return g_tbw.load(std::memory_order_relaxed); }
+
 static std::atomic<int> g_autotune{[] {
     const char* e = std::getenv("PYRSGM_GB300_AUTOTUNE");
     return e && std::atoi(e) != 0 ? 1 : 0;
@@ -432,6 +438,8 @@ int pyrsgm_gb300_set_packed_words(int words)
 }
 
 int pyrsgm_gb300_set_fused(int on) { return pg::g_fused.exchange(on ? 1 : 0, std::memory_order_relaxed); }
+
+int pyrsgm_gb300_set_tbw(int on) { return pg::g_tbw.exchange(on ? 1 : 0, std::memory_order_relaxed); }
 
 int pyrsgm_gb300_set_autotune(int on) { return pg::g_autotune.exchange(on ? 1 : 0, std::memory_order_relaxed); }
 

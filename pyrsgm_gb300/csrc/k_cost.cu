@@ -385,6 +385,20 @@ __device__ __forceinline__ int bt_pixel(const uint4 l, const uint4 r)
     return imin(255, (int)(t & 0xffffu) + (int)(t >> 18));
 }
 
+// The same cost plus kBtOff, for the tiled window sums.  With m = min(c0, c1)
+// (256 + bt in each half), m >> 18 = 64 + (bt(intensity) >> 2) lies in the
+// low half alone, so one __viaddmin_u16x2 adds it to 256 + bt(gradient),
+// clamps at 255 + kBtOff and zeroes the high half.  Sums of these carry
+// kBtOff per term, taken off once per label.
+constexpr uint32_t kBtOff = 320, kBtOffClamp = 255 + kBtOff;
+__device__ __forceinline__ uint32_t bt_pixel_off(const uint4 l, const uint4 r)
+{
+    const uint32_t c0 = __vimax3_u16x2(kBtBias2, l.x - r.w, r.z - l.y);
+    const uint32_t c1 = __vimax3_u16x2(kBtBias2, r.x - l.w, l.z - r.y);
+    const uint32_t m = __vminu2(c0, c1);
+    return __viaddmin_u16x2(m, m >> 18, kBtOffClamp);
+}
+
 // ---------------------------------------------------------------------------
 // BT coarse / single-scale cost: kernel_BTCost followed by kernel_BoxFilterH
 // and kernel_BoxFilterV (src/sgm_kernels.cu:139-239, 354-416), fused.  The
@@ -468,7 +482,9 @@ __global__ void __launch_bounds__(256) k_cost_bt_box(const __grid_constant__ Job
 //   phase 2: a thread per pixel adds blockSize rows of those sums, two
 //            labels per 32-bit add, from its own real-disparity offset.
 // Window sums are exact integers (at most 25 * 255 here, no intermediate
-// clamp in the reference).  Tiles whose parents disagree more widely are
+// clamp in the reference); the terms carry kBtOff each (bt_pixel_off), at
+// most 25 * 575 per 16-bit half, removed after the column sums.  Tiles
+// whose parents disagree more widely are
 // split into two base clusters (a pass each); pixels in neither, or a
 // wider window, evaluate each window directly.
 // ---------------------------------------------------------------------------
@@ -537,19 +553,19 @@ __device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, ui
         auto walk = [&](auto inner) {
             constexpr bool IN = decltype(inner)::value;
             const uint4* srl = rrow + c0 - ri + rn - 1;   // right feature of window column j: srl[j] (interior)
-            int q[2 * HW + 1];
+            uint32_t q[2 * HW + 1];
 #pragma unroll
             for (int i = 0; i < 2 * HW + 1; ++i) q[i] = 0;
-            int s = 0;
+            uint32_t s = 0;
 #pragma unroll
             for (int j = 0; j < SW; ++j) {
-                int e;
+                uint32_t e;   // cost + kBtOff
                 if (IN) {
-                    e = bt_pixel(lrow[j], srl[j]);
+                    e = bt_pixel_off(lrow[j], srl[j]);
                 } else {
                     const int gx = iclamp(x0 - HW + c0 + j, 0, W - 1);
                     const int x2 = gx - real;
-                    e = (x2 >= 0 && x2 < W) ? bt_pixel(lrow[j], rrow[x2 - xrs]) : 255;
+                    e = (x2 >= 0 && x2 < W) ? bt_pixel_off(lrow[j], rrow[x2 - xrs]) : kBtOffClamp;
                 }
                 s += e;
                 if (j >= 2 * HW && on) out[(j - 2 * HW) * kTiRs] = (uint16_t)s;
@@ -637,9 +653,11 @@ __global__ void __launch_bounds__(256, 3) k_cost_bt_tiled(const __grid_constant_
             int lo, hi;
             label_range(J, x, bq[i], lo, hi);
             int16_t* out = J.C + ((size_t)yq[i] * W + x) * D;
-            // packed pair sums of 2h+1 rows from offset ri0 = b - rmin (halves), 8 labels per chunk
+            // packed pair sums of 2h+1 rows from offset ri0 = b - rmin (halves), 8 labels per chunk;
+            // each half carries kBtOff per window pixel
             const int ri0 = bq[i] - rmin;
             const uint32_t sh = (uint32_t)(ri0 & 1) * 16;
+            const uint32_t off2 = (kBtOff * (uint32_t)((2 * h + 1) * (2 * h + 1))) * 0x10001u;
             for (int d0 = 0; d0 < D; d0 += 8) {
                 uint32_t acc[5] = {0u, 0u, 0u, 0u, 0u};
                 for (int k = 0; k <= 2 * h; ++k) {
@@ -651,7 +669,7 @@ __global__ void __launch_bounds__(256, 3) k_cost_bt_tiled(const __grid_constant_
                 uint32_t w[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    w[q] = __funnelshift_r(acc[q], acc[q + 1], sh);
+                    w[q] = __funnelshift_r(acc[q], acc[q + 1], sh) - off2;
                     const int d = d0 + 2 * q;
                     if (d < lo || d > hi) w[q] = (w[q] & 0xffff0000u) | (uint32_t)kMax;
                     if (d + 1 < lo || d + 1 > hi) w[q] = (w[q] & 0xffffu) | ((uint32_t)kMax << 16);

@@ -555,7 +555,6 @@ bool fused_applicable(const Jobs<NJ>& jobs)
     return jobs.n > 0;
 }
 
-int fused_mode();   // 1: use the fused passes where applicable (default), 0: never
 
 template <int NJ>
 cudaError_t launch_paths_fused16(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)

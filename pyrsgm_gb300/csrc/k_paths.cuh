@@ -824,7 +824,7 @@ cudaError_t launch_paths_mode(const Jobs<NJ>& jobs, const LevelExtent& e, cudaSt
     // fused T->B + L->R and R->L + WTA passes (k_fused.cuh)
     bool fused = false;
     if constexpr (PYR) fused = D == 16 && fused_mode() != 0 && fused_applicable(jobs);
-    const TuneKey key{D, PYR ? (fused ? 2 : 1) : 0, (int)std::min<long long>(rows, INT_MAX), e.max_w};
+    const TuneKey key{D, PYR ? (fused ? 2 : D == 16 && tbw_mode() ? 3 : 1) : 0, (int)std::min<long long>(rows, INT_MAX), e.max_w};
     cudaError_t err = cudaSuccess;
     switch (path_variant(D)) {
     case 10016: {

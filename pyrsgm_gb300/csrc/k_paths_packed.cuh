@@ -56,6 +56,7 @@
 #include "sgm_launch.h"
 
 namespace pg {
+
 namespace pk {
 
 constexpr uint32_t kMax2 = 0x7fff7fffu;
@@ -259,6 +260,58 @@ __device__ __forceinline__ uint32_t gcombine(uint32_t a, uint32_t b)
     } else {
         return __viaddmin_u16x2(a, b, kMax2);
     }
+}
+
+// Three-path total of one word (labels 2i, 2i+1) at a pyramid level: the
+// sum clamped at SHRT_MAX - 1, SHRT_MAX where any path is SHRT_MAX -- the
+// same as two gcombine<true>, in seven instructions instead of fourteen.
+__device__ __forceinline__ uint32_t gtotal3(uint32_t a, uint32_t b, uint32_t c)
+{
+    const uint32_t s = __viaddmin_u16x2(__viaddmin_u16x2(b, c, 0x7ffe7ffeu), a, 0x7ffe7ffeu);
+    return s | (sign_mask2(__vimax3_u16x2(a, b, c) + kOne2) & kMax2);
+}
+
+// Half j (0..15, not a compile-time constant) of 8 packed words, by a
+// select tree on the bits of j: no indexed access, so the words stay in
+// registers.
+__device__ __forceinline__ int half_of(const uint32_t (&t)[8], int j)
+{
+    const bool b1 = j & 2, b2 = j & 4, b3 = j & 8;
+    const uint32_t p0 = b1 ? t[1] : t[0], p1 = b1 ? t[3] : t[2], p2 = b1 ? t[5] : t[4], p3 = b1 ? t[7] : t[6];
+    const uint32_t q0 = b2 ? p1 : p0, q1 = b2 ? p3 : p2;
+    const uint32_t w = b3 ? q1 : q0;
+    return (int)((w >> ((j & 1) * 16)) & 0xffffu);
+}
+
+// Winner over 16 packed labels, as k_wta defines it: minimum cost and the
+// first label reaching it (minimum of the keys cost << 4 | label), the
+// minimum cost over labels farther than one from it, and the costs next to
+// it (0 outside the range).
+__device__ __forceinline__ void wta16(const uint32_t (&t)[8], int& minCost, int& bestD, int& alt, int& c0, int& c2)
+{
+    uint32_t k[16];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        k[2 * i] = ((t[i] << 4) & 0xffff0u) | (uint32_t)(2 * i);
+        k[2 * i + 1] = ((t[i] >> 12) & 0xffff0u) | (uint32_t)(2 * i + 1);
+    }
+    auto min16 = [](const uint32_t (&v)[16]) {
+        const uint32_t a = __vimin3_u32(v[0], v[1], v[2]), b = __vimin3_u32(v[3], v[4], v[5]);
+        const uint32_t c = __vimin3_u32(v[6], v[7], v[8]), d = __vimin3_u32(v[9], v[10], v[11]);
+        const uint32_t e = __vimin3_u32(v[12], v[13], v[14]);
+        const uint32_t x = __vimin3_u32(a, b, c), y = __vimin3_u32(d, e, v[15]);
+        return x < y ? x : y;
+    };
+    const uint32_t best = min16(k);
+    minCost = (int)(best >> 4);
+    bestD = (int)(best & 15u);
+    const int nb = 1 - bestD;
+    uint32_t far[16];
+#pragma unroll
+    for (int d = 0; d < 16; ++d) far[d] = (unsigned)(d + nb) <= 2u ? 0xffffffffu : k[d];
+    alt = (int)(min16(far) >> 4);
+    c0 = bestD > 0 ? half_of(t, bestD - 1) : 0;
+    c2 = bestD < 15 ? half_of(t, bestD + 1) : 0;
 }
 
 // Outputs of a winner (kernel_WTA_Subpixel, src/sgm_kernels.cu:573-640;
@@ -864,6 +917,138 @@ __global__ void __launch_bounds__(256) k_wta(const __grid_constant__ Jobs<NJ> jo
     wta_out<D, PYR>(J, y, x, base, minCost, bestD, alt, c0, minCost, c2);
 }
 
+// ---------------------------------------------------------------------------
+// Top -> bottom with the winner-take-all folded in: 16-label pyramid levels
+// with all three paths, one thread per column chain, run after the row
+// pass.  Each step a chain reads, beside its pixel's costs, the pixel's
+// L->R and R->L path costs through the same cp.async ring, adds its own
+// T->B costs to them (the one-cap sum is order-free) and picks the winner
+// exactly as k_wta does.  The T->B costs are neither written nor read
+// again: 96 bytes per pixel in plus the outputs, against 64 for k_gtb and
+// 96 for k_wta.  Three ring slots of 3 x 1 KB per warp keep 16 warps per
+// SM resident, enough for the 1080p level of 32 pairs in one wave.
+// ---------------------------------------------------------------------------
+namespace pk {
+constexpr int kStagesTbw = 3;
+
+__host__ __device__ constexpr size_t tbw_smem()
+{
+    using G = Grp<8, 1>;
+    return 256 * 4 + (size_t)4 * 4 * (G::BUFW + kStagesTbw * 3 * 256 + kStagesTbw * 64);
+}
+}  // namespace pk
+
+template <int NJ>
+__global__ void __launch_bounds__(128, 4) k_gtbw(const __grid_constant__ Jobs<NJ> jobs)
+{
+    using namespace pk;
+    using G = Grp<8, 1>;
+    constexpr int D = 16, S = kStagesTbw, kWarps = 4, SLOT = 3 * 256;   // words: costs, Vl, Vr of 32 lanes
+    const LevelDesc& J = jobs.d[blockIdx.y];
+    extern __shared__ __align__(16) uint32_t smem[];
+    int* lut = reinterpret_cast<int*>(smem);
+    uint32_t* cbuf = smem + 256;
+    uint32_t* rbuf = cbuf + kWarps * G::BUFW;
+    uint32_t* bibuf = rbuf + kWarps * S * SLOT;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = J.adaptive ? J.p2lut[i] : 0;
+    for (int i = threadIdx.x; i < kWarps * G::BUFW; i += blockDim.x) cbuf[i] = kMax2;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int W = J.w, H = J.h;
+    const int col0 = (blockIdx.x * kWarps + warp) * 32;
+    if (col0 >= W) return;   // the whole warp is past the image
+    const int col = col0 + lane;
+    const bool col_ok = col < W;
+    const int x = imin(col, W - 1);
+    uint32_t* chain = cbuf + warp * G::BUFW + lane;
+    uint32_t* ring = rbuf + warp * S * SLOT + lane * 8;
+    uint32_t* bi = bibuf + warp * S * 64 + lane;   // [slot][base, image][lane]
+    const int h0 = ring_half(0, lane), h1 = ring_half(1, lane);
+    const uint32_t p12 = dup(imin(J.P1, 0x8000));
+    int lo = 0, hi = D - 1;
+    if (!J.refine) label_range(J, x, J.minD, lo, hi);
+    const bool use_base = J.refine != 0, adaptive = J.adaptive != 0;
+    const int16_t* const Cg = J.C;
+    const int16_t* const Lp = J.Vl;
+    const int16_t* const Rp = J.Vr;
+    const int16_t* const Bg = J.base;
+    const uint8_t* const Lg = J.left;
+    const size_t vstep = (size_t)W * D, lstep = (size_t)J.lstep;
+    size_t oi = (size_t)x * D, pi = x, li = x;   // issue cursor (row yi)
+    size_t pc = pi, lc = li;                     // consume cursor (row y)
+    int yi = 0;
+    auto issue_next = [&](int slot) {
+        if (yi < H) {
+            uint32_t* d = ring + slot * SLOT;
+            cp16(d + h0, Cg + oi);
+            cp16(d + h1, Cg + oi + 8);
+            cp16(d + 256 + h0, Lp + oi);
+            cp16(d + 256 + h1, Lp + oi + 8);
+            cp16(d + 512 + h0, Rp + oi);
+            cp16(d + 512 + h1, Rp + oi + 8);
+            if (use_base) cp4(bi + slot * 64, word_of(Bg + pi));
+            if (adaptive) cp4(bi + slot * 64 + 32, word_of(Lg + li));
+        }
+        cp_commit();
+        ++yi;
+        oi += vstep;
+        pi += W;
+        li += lstep;
+    };
+    auto ld8 = [&](const uint32_t* d, uint32_t (&v)[8]) {
+        const uint4 a = *reinterpret_cast<const uint4*>(d + h0);
+        const uint4 b = *reinterpret_cast<const uint4*>(d + h1);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    };
+    GChain<8> s;
+    gchain_init(s, J.minD);
+#pragma unroll
+    for (int j = 0; j < S - 1; ++j) issue_next(j);
+    int img_prev = 0, slot = 0, islot = S - 1;
+    for (int y = 0; y < H; ++y) {
+        issue_next(islot);
+        islot = islot + 1 == S ? 0 : islot + 1;
+        cp_wait<S - 1>();
+        const uint32_t* d = ring + slot * SLOT;
+        const uint32_t* db = bi + slot * 64;
+        slot = slot + 1 == S ? 0 : slot + 1;
+        uint32_t cc[8], t[8];
+        ld8(d, cc);
+        const int base = use_base ? (int)(int16_t)(db[0] >> ((pc & 1) * 16)) : J.minD;
+        int p2 = J.P2;
+        if (adaptive) {
+            const int img = (int)((db[32] >> byte_shift(Lg + lc)) & 255u);
+            p2 = lut[abs(img - img_prev) & 255];
+            img_prev = img;
+        }
+        if (!J.refine) mask_labels<8>(cc, lo, hi, 0);
+        gstep<8, 1, true>(s, cc, base, p2, p12, chain, 0);
+        {
+            uint32_t u[8];
+            ld8(d + 512, t);   // R->L
+            ld8(d + 256, u);   // L->R
+#pragma unroll
+            for (int i = 0; i < 8; ++i) t[i] = gtotal3(s.L[i], u[i], t[i]);
+        }
+        if (col_ok) {
+            const size_t p = (size_t)y * W + x;
+            if (J.debug_acc) {
+                reinterpret_cast<uint4*>(J.V + p * D)[0] = make_uint4(t[0], t[1], t[2], t[3]);
+                reinterpret_cast<uint4*>(J.V + p * D)[1] = make_uint4(t[4], t[5], t[6], t[7]);
+            }
+            int minCost, bestD, alt, c0, c2;
+            wta16(t, minCost, bestD, alt, c0, c2);
+            wta_out<D, true>(J, y, x, base, minCost, bestD, alt, c0, minCost, c2);
+        }
+        pc += W;
+        lc += lstep;
+    }
+    cp_wait<0>();
+}
+
+
+
 template <int NW, int T, bool PYR, int NJ>
 cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t st)
 {
@@ -876,9 +1061,17 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     // runs on a second stream beside the row pass, joined before the WTA;
     // launches that fill the GPU run them one after the other (side by side
     // they only contend).
+    // 16-label pyramid levels, wide shape, three paths everywhere: the row
+    // pass first, then T->B with the winner-take-all (k_gtbw)
+    bool tbw = false;
+    if constexpr (PYR && NW == 8 && T == 1) {
+        tbw = tbw_mode() != 0;
+        for (int i = 0; i < jobs.n; ++i) tbw = tbw && jobs.d[i].paths >= 3;
+    }
     ForkStreams& fk = fork_streams(st);
     const bool fork = NW != 8 && any_tb && fk.aux != nullptr;
     cudaStream_t tbst = st;
+    if (tbw) any_tb = false;
     if (fork) {
         if ((err = cudaEventRecord(fk.fork, st)) != cudaSuccess) return err;
         if ((err = cudaStreamWaitEvent(fk.aux, fk.fork, 0)) != cudaSuccess) return err;
@@ -938,6 +1131,21 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     if (fork) {
         if ((err = cudaEventRecord(fk.join, fk.aux)) != cudaSuccess) return err;
         if ((err = cudaStreamWaitEvent(st, fk.join, 0)) != cudaSuccess) return err;
+    }
+    if constexpr (PYR && NW == 8 && T == 1) {
+        if (tbw) {
+            constexpr size_t smem = pk::tbw_smem();
+            if ((err = cudaFuncSetAttribute(k_gtbw<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+                cudaSuccess)
+                return err;
+            dim3 gt((e.max_w + 127) / 128, jobs.n);
+            prof_begin(st);
+            k_gtbw<NJ><<<gt, 128, smem, st>>>(jobs);
+            count_launch();
+            prof_end(PK_TBW, jobs_vox(jobs) * 6 + jobs_px(jobs) * ((jobs.d[0].refine ? 2 : 0) + (jobs.d[0].adaptive ? 1 : 0) + 10),
+                     st);
+            return cudaGetLastError();
+        }
     }
     dim3 gw((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
     prof_begin(st);

@@ -18,6 +18,7 @@ enum ProfKind {
     PK_WTA = 8,
     PK_TBLR = 9,   // fused T->B + L->R pass (16-label pyramid levels)
     PK_RLW = 10,   // fused R->L + winner-take-all pass
+    PK_TBW = 11,   // T->B pass with the winner-take-all folded in
     PK_COUNT
 };
 

@@ -101,6 +101,10 @@ ForkStreams& fork_streams(cudaStream_t st);
 int packed_words_override();
 // Warps per SM the NW = 8 shape must fill before a launch takes it.
 int packed_min_warps_per_sm();
+// 1: fused two-pass form of the 16-label pyramid levels (opt-in).
+int fused_mode();
+// 1: T->B pass with the winner-take-all for those levels (default).
+int tbw_mode();
 
 // Measuring shape choice for the 16/32/64-label aggregation (opt-in,
 // pyrsgm_gb300_set_autotune).  A launch is keyed by its label count, mode,

@@ -112,12 +112,19 @@ def _c3_params(cost, levels):
                 pyramid_coarse_disparities=128)
 
 
-@pytest.mark.parametrize("words", [0, 8])
-def test_c3_1920x1080_d256_bt_three_levels(words):
+@pytest.mark.parametrize("words,tbw", [(0, True), (8, True), (8, False)], ids=["auto", "wide", "wide_three_pass"])
+def test_c3_1920x1080_d256_bt_three_levels(words, tbw):
+    """The 16-label levels with the winner-take-all in the T->B pass (the
+    default) and in a pass of its own."""
+    import pyrsgm_gb300 as pg
     _need_ref()
     left, right = _pair(1920, 1080, 255, 16, 3001)
-    _check_levels(_with_words(words, lambda: _runners.matcher_levels(
-        1920, 1080, _c3_params(cases.BT, 3), left, right)))
+    prev = pg.set_tbw(tbw)
+    try:
+        records = _with_words(words, lambda: _runners.matcher_levels(1920, 1080, _c3_params(cases.BT, 3), left, right))
+    finally:
+        pg.set_tbw(prev)
+    _check_levels(records)
 
 
 @pytest.mark.parametrize("words", [0, 8])

@@ -87,30 +87,34 @@ PACKED = [c for c in cases.SINGLE_SCALE + cases.LEVELS if c["D"] in (16, 32, 64)
 
 
 # kernel shapes of the 16/32/64-label aggregation: (words per thread, fused
-# passes for 16-label pyramid levels)
-SHAPES = [(8, True), (8, False), (2, True)]
-SHAPE_IDS = ["wide_fused", "wide", "spread"]
+# passes for 16-label pyramid levels, T->B pass with the winner-take-all for
+# 16-label pyramid levels)
+SHAPES = [(8, True, True), (8, False, True), (8, False, False), (2, True, True)]
+SHAPE_IDS = ["wide_fused", "wide", "wide_three_pass", "spread"]
 
 
-def _run_shape(case, words, fused):
+def _run_shape(case, words, fused, tbw):
     import pyrsgm_gb300 as pg
     prev = pg.set_packed_words(words)
     prev_f = pg.set_fused(fused)
+    prev_t = pg.set_tbw(tbw)
     try:
         return _runners.run_mine(case)
     finally:
         pg.set_packed_words(prev)
         pg.set_fused(prev_f)
+        pg.set_tbw(prev_t)
 
 
-@pytest.mark.parametrize("words,fused", SHAPES, ids=SHAPE_IDS)
+@pytest.mark.parametrize("words,fused,tbw", SHAPES, ids=SHAPE_IDS)
 @pytest.mark.parametrize("case", PACKED, ids=[c["name"] for c in PACKED])
-def test_packed_shapes_match_reference(case, words, fused):
-    """Every shape of the 16/32/64-label kernels (one thread per 16 labels,
-    the fused two-pass form of the 16-label pyramid levels, or a chain spread
+def test_packed_shapes_match_reference(case, words, fused, tbw):
+    """Every shape of the 16/32/64-label kernels (one thread per 16 labels
+    with the winner-take-all in the T->B pass or in a pass of its own, the
+    fused two-pass form of the 16-label pyramid levels, or a chain spread
     over several threads) gives the reference's results."""
     import pyrsgm_gb300 as pg
-    mine = _run_shape(case, words, fused)
+    mine = _run_shape(case, words, fused, tbw)
     assert pg.fused_stalls() == 0
     if _oracle.ref_available():
         other = _runners.run_ref(case)
@@ -134,10 +138,10 @@ ODD_PACKED = [
 ]
 
 
-@pytest.mark.parametrize("words,fused", SHAPES, ids=SHAPE_IDS)
+@pytest.mark.parametrize("words,fused,tbw", SHAPES, ids=SHAPE_IDS)
 @pytest.mark.parametrize("case", ODD_PACKED, ids=[c["name"] for c in ODD_PACKED])
-def test_packed_shapes_odd_widths_match_reference(case, words, fused):
-    mine = _run_shape(case, words, fused)
+def test_packed_shapes_odd_widths_match_reference(case, words, fused, tbw):
+    mine = _run_shape(case, words, fused, tbw)
     if _oracle.ref_available():
         other = _runners.run_ref(case)
     else:
