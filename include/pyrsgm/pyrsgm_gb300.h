@@ -239,13 +239,15 @@ int pyrsgm_gb300_set_packed_words(int words);
 int pyrsgm_gb300_set_fused(int on);
 
 /* Winner-take-all inside the top-to-bottom pass for the 16-label pyramid
- * levels with three paths, in the one-thread-per-16-labels shape (on by
- * default; PYRSGM_GB300_TBW=0 turns it off at load).  When on, the row pass
- * runs first and the top-to-bottom chains add their costs to the row
+ * levels with three paths, in the one-thread-per-16-labels shape: the row
+ * pass runs first and the top-to-bottom chains add their costs to the row
  * paths' and pick the winners, instead of writing a top-to-bottom volume
- * for a separate winner-take-all pass; results are identical.  Returns the
- * previous setting. */
-int pyrsgm_gb300_set_tbw(int on);
+ * for a separate winner-take-all pass.  Mode 1 (default) takes this form
+ * for launches with columns for at least 9 warps per SM, where it is the
+ * faster one; 0 never, 2 always.  PYRSGM_GB300_TBW gives the initial mode.
+ * Results are identical.  Returns the previous mode, or -1 for another
+ * value. */
+int pyrsgm_gb300_set_tbw(int mode);
 
 /* Waits of the fused pass that ran out of time (a band whose band above
  * never published its edge; results of that launch are wrong), counted on

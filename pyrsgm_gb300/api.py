@@ -219,10 +219,15 @@ def set_fused(on: bool) -> bool:
     return bool(lib().pyrsgm_gb300_set_fused(1 if on else 0))
 
 
-def set_tbw(on: bool) -> bool:
+def set_tbw(mode: int) -> int:
     """Winner-take-all inside the top-to-bottom pass of the 16-label pyramid
-    levels (pyrsgm_gb300_set_tbw, on by default); returns the previous setting."""
-    return bool(lib().pyrsgm_gb300_set_tbw(1 if on else 0))
+    levels (pyrsgm_gb300_set_tbw): 0 never, 1 for launches that fill the GPU
+    (default), 2 always; returns the previous mode.  Results do not depend
+    on it."""
+    r = lib().pyrsgm_gb300_set_tbw(int(mode))
+    if r < 0:
+        raise ValueError("pyrsgm: tbw mode must be 0, 1 or 2")
+    return r
 
 
 def fused_stalls(reset: bool = False) -> int:

@@ -51,7 +51,8 @@ int fused_mode() { return g_fused.load(std::memory_order_relaxed); }
 
 static std::atomic<int> g_tbw{[] {
     const char* e = std::getenv("PYRSGM_GB300_TBW");
-    return e && std::atoi(e) == 0 ? 0 : 1;
+    const int v = e ? std::atoi(e) : 1;
+    return v >= 0 && v <= 2 ? v : 1;
 }()};
 int tbw_mode() { return g_tbw.load(std::memory_order_relaxed); }
 
@@ -439,7 +440,11 @@ int pyrsgm_gb300_set_packed_words(int words)
 
 int pyrsgm_gb300_set_fused(int on) { return pg::g_fused.exchange(on ? 1 : 0, std::memory_order_relaxed); }
 
-int pyrsgm_gb300_set_tbw(int on) { return pg::g_tbw.exchange(on ? 1 : 0, std::memory_order_relaxed); }
+int pyrsgm_gb300_set_tbw(int mode)
+{
+    if (mode < 0 || mode > 2) return -1;
+    return pg::g_tbw.exchange(mode, std::memory_order_relaxed);
+}
 
 int pyrsgm_gb300_set_autotune(int on) { return pg::g_autotune.exchange(on ? 1 : 0, std::memory_order_relaxed); }
 

@@ -472,13 +472,15 @@ __global__ void __launch_bounds__(256) k_cost_bt_box(const __grid_constant__ Job
 //   staging: the features of every window row of the tile (left: one per
 //            window column, clamped; right: the ones its disparities reach)
 //            are copied once into shared memory with cp.async;
-//   phase 1: the (window row, real disparity) pairs of a half row of 16
-//            output columns are numbered row-major and cut into units of
-//            32, one pair per lane, dealt to the 8 warps in turn; a lane
-//            walks its half row left to right and keeps the running sum of
-//            the last blockSize costs (sums along x, into shared memory).
-//            A tile usually needs 17 real disparities, so numbering the
-//            pairs this way keeps nearly every lane busy;
+//   phase 1: the (window row, two adjacent real disparities) units of a
+//            half row of 16 output columns are numbered row-major and cut
+//            into groups of 32, one unit per lane, dealt to the 8 warps in
+//            turn; a lane walks its half row left to right and keeps the
+//            running sums of the last blockSize costs of both disparities
+//            (sums along x, into shared memory), loading each left and
+//            right feature once for the two.  A tile usually needs 17 real
+//            disparities, so numbering the units this way keeps nearly
+//            every lane busy;
 //   phase 2: a thread per pixel adds blockSize rows of those sums, two
 //            labels per 32-bit add, from its own real-disparity offset.
 // Window sums are exact integers (at most 25 * 255 here, no intermediate
@@ -538,44 +540,64 @@ __device__ __forceinline__ void bt_row_sums(const LevelDesc& J, uint16_t* hs, ui
     __syncthreads();
     // every window column of the tile inside the image, and every right pixel too
     const bool interior = x0 - HW >= 0 && x0 + kTiX - 1 + HW < W && xrs >= 0 && xrs + nsr - 1 < W;
-    const int pairs = R * rn;                      // (window row, real disparity) pairs of a half row
+    // Units: (window row, real-disparity pair ri, ri + 1) of a half row,
+    // numbered row-major, one per lane.  Real disparity ri + 1 needs at
+    // window column j the right feature that ri needed at column j - 1, so
+    // a lane loads one left and one right feature per column for two sums
+    // and stores both as one word.  With rn odd the last pair's second
+    // half is past the cluster: computed, never read.
+    const int rp = (rn + 1) >> 1;
+    const int pairs = R * rp;
     const int chunks = (pairs + 31) >> 5;
     for (int u = warp; u < 2 * chunks; u += kTiWarps) {
         const int seg = u & 1, f = (u >> 1) * 32 + lane;
         const bool on = f < pairs;
         const int fr = on ? f : pairs - 1;
-        const int row = fr / rn, ri = fr - row * rn;
+        const int row = fr / rp, ri = 2 * (fr - row * rp);
         const int real = rmin + ri;
         const int c0 = seg * kTiSeg;               // first window column of the half row (tile-relative)
         const uint4* lrow = sl + row * kTiSL + c0;
         const uint4* rrow = sr + row * kTiSR;
-        uint16_t* out = hs + ((size_t)row * kTiX + c0) * kTiRs + ri;
+        uint32_t* out = reinterpret_cast<uint32_t*>(hs + ((size_t)row * kTiX + c0) * kTiRs + ri);
         auto walk = [&](auto inner) {
             constexpr bool IN = decltype(inner)::value;
-            const uint4* srl = rrow + c0 - ri + rn - 1;   // right feature of window column j: srl[j] (interior)
-            uint32_t q[2 * HW + 1];
+            // right feature of window column j for ri: srl[j]; for ri + 1: srl[j - 1] (interior)
+            const uint4* srl = rrow + c0 - ri + rn - 1;
+            uint4 rprev = IN ? srl[-1] : make_uint4(0u, 0u, 0u, 0u);
+            uint32_t q0[2 * HW + 1], q1[2 * HW + 1];
 #pragma unroll
-            for (int i = 0; i < 2 * HW + 1; ++i) q[i] = 0;
-            uint32_t s = 0;
+            for (int i = 0; i < 2 * HW + 1; ++i) q0[i] = q1[i] = 0;
+            uint32_t s0 = 0, s1 = 0;
 #pragma unroll
             for (int j = 0; j < SW; ++j) {
-                uint32_t e;   // cost + kBtOff
+                uint32_t e0, e1;   // costs + kBtOff at real disparities ri, ri + 1
                 if (IN) {
-                    e = bt_pixel_off(lrow[j], srl[j]);
+                    const uint4 l = lrow[j], r = srl[j];
+                    e0 = bt_pixel_off(l, r);
+                    e1 = bt_pixel_off(l, rprev);
+                    rprev = r;
                 } else {
                     const int gx = iclamp(x0 - HW + c0 + j, 0, W - 1);
-                    const int x2 = gx - real;
-                    e = (x2 >= 0 && x2 < W) ? bt_pixel_off(lrow[j], rrow[x2 - xrs]) : kBtOffClamp;
+                    const int x2 = gx - real, x3 = x2 - 1;
+                    const uint4 l = lrow[j];
+                    e0 = (x2 >= 0 && x2 < W) ? bt_pixel_off(l, rrow[x2 - xrs]) : kBtOffClamp;
+                    e1 = (x3 >= 0 && x3 < W) ? bt_pixel_off(l, rrow[x3 - xrs]) : kBtOffClamp;
                 }
-                s += e;
-                if (j >= 2 * HW && on) out[(j - 2 * HW) * kTiRs] = (uint16_t)s;
+                s0 += e0;
+                s1 += e1;
+                if (j >= 2 * HW && on) out[(j - 2 * HW) * (kTiRs / 2)] = s0 | (s1 << 16);
                 if (HW > 0) {
-                    s -= q[0];
+                    s0 -= q0[0];
+                    s1 -= q1[0];
 #pragma unroll
-                    for (int i = 0; i + 1 < 2 * HW; ++i) q[i] = q[i + 1];
-                    q[2 * HW - 1 < 0 ? 0 : 2 * HW - 1] = e;
+                    for (int i = 0; i + 1 < 2 * HW; ++i) {
+                        q0[i] = q0[i + 1];
+                        q1[i] = q1[i + 1];
+                    }
+                    q0[2 * HW - 1 < 0 ? 0 : 2 * HW - 1] = e0;
+                    q1[2 * HW - 1 < 0 ? 0 : 2 * HW - 1] = e1;
                 } else {
-                    s = 0;
+                    s0 = s1 = 0;
                 }
             }
         };

@@ -930,6 +930,7 @@ __global__ void __launch_bounds__(256) k_wta(const __grid_constant__ Jobs<NJ> jo
 // ---------------------------------------------------------------------------
 namespace pk {
 constexpr int kStagesTbw = 3;
+constexpr int kTbwMinWarpsPerSm = 9;
 
 __host__ __device__ constexpr size_t tbw_smem()
 {
@@ -1061,12 +1062,22 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     // runs on a second stream beside the row pass, joined before the WTA;
     // launches that fill the GPU run them one after the other (side by side
     // they only contend).
-    // 16-label pyramid levels, wide shape, three paths everywhere: the row
-    // pass first, then T->B with the winner-take-all (k_gtbw)
+    // 16-label pyramid levels, wide shape, three paths everywhere, and
+    // columns for at least kTbwMinWarpsPerSm warps per SM: the row pass
+    // first, then T->B with the winner-take-all (k_gtbw).  Its serial chain
+    // step carries the winner's work, so with few warps per SM it loses to
+    // k_gtb + k_wta: per launch, 16 pairs of 1080p, 1165 against 1031 us
+    // at 6.3 warps per SM and 467 against 308 us at 3.2; at 12.6 warps per
+    // SM (32 pairs) it is about 15 % faster.
     bool tbw = false;
     if constexpr (PYR && NW == 8 && T == 1) {
+        long long cols = 0;
         tbw = tbw_mode() != 0;
-        for (int i = 0; i < jobs.n; ++i) tbw = tbw && jobs.d[i].paths >= 3;
+        for (int i = 0; i < jobs.n; ++i) {
+            tbw = tbw && jobs.d[i].paths >= 3;
+            cols += jobs.d[i].w;
+        }
+        tbw = tbw && (tbw_mode() == 2 || cols >= 32LL * pk::kTbwMinWarpsPerSm * sm_count());
     }
     ForkStreams& fk = fork_streams(st);
     const bool fork = NW != 8 && any_tb && fk.aux != nullptr;

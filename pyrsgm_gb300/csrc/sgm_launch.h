@@ -103,7 +103,8 @@ int packed_words_override();
 int packed_min_warps_per_sm();
 // 1: fused two-pass form of the 16-label pyramid levels (opt-in).
 int fused_mode();
-// 1: T->B pass with the winner-take-all for those levels (default).
+// T->B pass with the winner-take-all for those levels: 0 never, 1 when a
+// launch fills the GPU (default), 2 always.
 int tbw_mode();
 
 // Measuring shape choice for the 16/32/64-label aggregation (opt-in,

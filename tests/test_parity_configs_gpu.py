@@ -112,7 +112,7 @@ def _c3_params(cost, levels):
                 pyramid_coarse_disparities=128)
 
 
-@pytest.mark.parametrize("words,tbw", [(0, True), (8, True), (8, False)], ids=["auto", "wide", "wide_three_pass"])
+@pytest.mark.parametrize("words,tbw", [(0, 1), (8, 2), (8, 0)], ids=["auto", "wide", "wide_three_pass"])
 def test_c3_1920x1080_d256_bt_three_levels(words, tbw):
     """The 16-label levels with the winner-take-all in the T->B pass (the
     default) and in a pass of its own."""

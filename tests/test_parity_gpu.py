@@ -87,9 +87,9 @@ PACKED = [c for c in cases.SINGLE_SCALE + cases.LEVELS if c["D"] in (16, 32, 64)
 
 
 # kernel shapes of the 16/32/64-label aggregation: (words per thread, fused
-# passes for 16-label pyramid levels, T->B pass with the winner-take-all for
-# 16-label pyramid levels)
-SHAPES = [(8, True, True), (8, False, True), (8, False, False), (2, True, True)]
+# passes for 16-label pyramid levels, mode of the T->B pass with the
+# winner-take-all for 16-label pyramid levels: 2 always, 0 never)
+SHAPES = [(8, True, 1), (8, False, 2), (8, False, 0), (2, True, 1)]
 SHAPE_IDS = ["wide_fused", "wide", "wide_three_pass", "spread"]
 
 
