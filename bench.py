@@ -53,13 +53,15 @@ def params_for(cost: int) -> dict:
                 pyramid_coarse_disparities=128)
 
 
-# Measured DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of
-# the aggregation launches per byte they move by their own design, from the
-# full capture of the level-0 launches of four 1080p pairs
-# (profiles/stage_kernels_1080p_4pairs.md): k_gtb 513 + k_grow 1037 + k_wta
-# 914 MB against 556 + 1112 + 912 MB of their own bytes.  Scaled to a step
-# by those bytes (every kernel streams its volumes once per launch).
-AGG_TRAFFIC_PER_ALG_BYTE = 2464.0 / 2580.0
+# Measured DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per
+# byte the aggregation kernels move by their own design, from the full
+# captures of the 1080p-level launches of eight pairs
+# (profiles/stage_kernels_1080p_8pairs.md): k_gtb 1066.8, k_grow 2147.6,
+# k_wta 1834.9 and k_gtbw 1854.7 MB against 1111.5, 2222.9, 1791.6 and
+# 1808.2 MB of their own bytes.  Every kernel streams its volumes once per
+# launch, so the ratio carries over to a step by each kind's own bytes.
+AGG_TRAFFIC_PER_OWN_BYTE = {"path_tb": 1066.8 / 1111.5, "path_row": 2147.6 / 2222.9, "wta": 1834.9 / 1791.6,
+                            "tbw": 1854.7 / 1808.2}
 
 
 def alg_bytes(width: int, height: int, params: dict) -> dict:
@@ -555,9 +557,9 @@ def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, 
         pr[...] = r
         host_pool.append((pl, pr, c))
     pairs_pool = host_pool
-    # the server's pool keeps plans of every shape resident (a plan
-    # allocated inside the timed stream would stall the lanes), then every
-    # pool pair runs once
+    # the server keeps plans of every shape and I/O buffers of every size
+    # resident (an allocation inside the timed stream would stall the
+    # lanes), then the pool runs in bursts
     counts = {}
     for l, _, c in pairs_pool:
         key = (l.shape[1], l.shape[0], c)
@@ -740,8 +742,10 @@ def result_line(args, world: int, headline: dict, plain: dict, pk: dict, npairs:
             "algorithmic": "4 B per voxel (partial aggregated volume written and read once as int16)",
             "alg_bytes_per_step": round(agg_alg / 1e9, 4),
             "implementation_bytes_per_step": round(own / 1e9, 4),
-            "traffic": round(AGG_TRAFFIC_PER_ALG_BYTE * own / 1e9, 4) if AGG_TRAFFIC_PER_ALG_BYTE else None,
-            "traffic_unit": "GB per step (ncu DRAM bytes per implementation byte x implementation bytes)",
+            "traffic": round(sum(AGG_TRAFFIC_PER_OWN_BYTE[k] * prof[k]["bytes"] for k in agg_keys) / ps / 1e9, 4)
+            if all(k in AGG_TRAFFIC_PER_OWN_BYTE for k in agg_keys) else None,
+            "traffic_unit": "GB per step (per kernel kind: ncu DRAM bytes per implementation byte x its "
+                            "implementation bytes)",
             "ms_per_step": round(agg_ms, 4), "launches_per_step": agg_launches,
             "avg_launch_ms": round(agg_ms / agg_launches, 5) if agg_launches else None}
         step_ms = headline["total_ms"] / args.steps

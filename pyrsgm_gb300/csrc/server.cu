@@ -2,8 +2,10 @@
 // reference (one pair per blocking-free call, no request handling).
 //
 // Requests carry host images and host output buffers.  A scheduler thread
-// forms a batch from whatever has arrived as soon as one of the server's
-// stream lanes is free (up to max_batch pairs and the lane's device budget),
+// forms a batch from whatever has arrived once one of the server's stream
+// lanes is free and the kernels of the batch before are done, or at once
+// when a full batch is queued (up to max_batch pairs and the lane's device
+// budget),
 // copies the inputs on the lane's stream, runs the lane's batch engine on
 // the compute stream that all lanes share (after the inputs) and copies the
 // outputs back on the lane's stream (after the kernels), all
@@ -318,16 +320,25 @@ public:
         inject_ += n;
     }
 
-    // Page-lock a host range so that requests whose images or outputs lie
-    // inside it are copied without staging.
-    // Plans for `count` pairs of one shape on every lane (allocated now;
-    // each lane's engine serialises this with its runs).
+    // Plans for `count` pairs of one shape in the shared engine, and device
+    // and pinned I/O buffers for `count` pairs of that size on every lane,
+    // allocated now: a batch of up to `count` such pairs then allocates
+    // nothing (a cudaHostAlloc inside the stream stalls the scheduler for
+    // milliseconds).
     int reserve(int w, int h, const pyrsgm_gb300_params& prm, int count, std::string& err)
     {
         try {
             const pyrsgm::Params p = toParams(prm);
             batch_engine_reserve(eng_, w, h, p, count, cst_);
             if (cudaStreamSynchronize(cst_) != cudaSuccess) throw std::runtime_error("reserve: stream error");
+            std::lock_guard<std::mutex> lk(pool_mu_);
+            for (auto& L : lanes_) {
+                auto& vec = L->pool[{w, h}];
+                while ((int)vec.size() < count) {
+                    vec.emplace_back(new IOBuf());
+                    vec.back()->alloc(w, h);
+                }
+            }
             return 0;
         } catch (const std::exception& e) {
             err = e.what();
@@ -335,6 +346,8 @@ public:
         }
     }
 
+    // Page-lock a host range so that requests whose images or outputs lie
+    // inside it are copied without staging.
     int register_host(void* p, size_t bytes, std::string& err)
     {
         if (!p || bytes == 0) {
@@ -420,6 +433,7 @@ private:
 
     IOBuf* take_buf(Lane& L, int w, int h, std::map<std::pair<int, int>, int>& used)
     {
+        std::lock_guard<std::mutex> lk(pool_mu_);
         auto& vec = L.pool[{w, h}];
         int& k = used[{w, h}];
         if ((int)vec.size() <= k) {
@@ -441,11 +455,15 @@ private:
                 cv_.wait(lk, [&] {
                     if (stop_) return true;
                     if (queue_.empty()) return false;
-                    // a batch is formed once no earlier batch is still computing:
-                    // what arrives meanwhile joins it instead of waiting behind
-                    // it in a small batch of its own
-                    for (auto& l : lanes_)
-                        if (l->computing) return false;
+                    // a batch is formed once no earlier batch is still computing
+                    // (what arrives meanwhile joins it instead of waiting behind
+                    // it in a small batch of its own), or at once when a full
+                    // batch is queued: then its input copies overlap the
+                    // kernels before it, and its kernels follow them on the
+                    // compute stream
+                    bool computing = false;
+                    for (auto& l : lanes_) computing = computing || l->computing;
+                    if (computing && (int)queue_.size() < max_batch_) return false;
                     for (auto& l : lanes_)
                         if (!l->busy) return true;
                     return false;
@@ -664,6 +682,7 @@ private:
     cudaStream_t cst_ = nullptr;   // compute stream shared by the lanes
     BatchEngine* eng_ = nullptr;   // pair plans and graphs shared by the lanes
     std::mutex reg_mu_;
+    std::mutex pool_mu_;   // the lanes' I/O buffer pools (scheduler and reserve())
     std::map<uintptr_t, size_t> reg_;   // registered host ranges: start -> bytes
     size_t lane_budget_ = 0;
     std::vector<std::unique_ptr<Lane>> lanes_;

@@ -215,6 +215,31 @@ def test_autotune_switch_and_empty_table_without_device_work():
         pg.set_autotune(prev)
 
 
+def test_kernel_form_switches_without_device_work():
+    """The three-way T->B winner switch and the fused switch set and return
+    their previous values; out-of-range modes are refused."""
+    import pytest
+    import pyrsgm_gb300 as pg
+    from pyrsgm_gb300._native import lib
+    prev = pg.set_tbw(2)
+    try:
+        assert pg.set_tbw(0) == 2
+        assert pg.set_tbw(1) == 0
+        assert lib().pyrsgm_gb300_set_tbw(3) == -1
+        assert lib().pyrsgm_gb300_set_tbw(-1) == -1
+        assert pg.set_tbw(1) == 1
+        with pytest.raises(ValueError):
+            pg.set_tbw(7)
+    finally:
+        pg.set_tbw(prev)
+    prev_f = pg.set_fused(True)
+    try:
+        assert pg.set_fused(False) is True
+        assert pg.set_fused(False) is False
+    finally:
+        pg.set_fused(prev_f)
+
+
 def test_new_entry_points_reject_bad_arguments_without_device_work():
     """Speckle filter, plan reservation and the autotune table check their
     arguments before any device call."""
