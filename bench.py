@@ -11,9 +11,10 @@ reference's headline metric is quoted on).
           the compute stream, L2 flushed between steps outside the events)
   e2e     the same through the public API with pinned host buffers: every
           step copies its pairs' images host->device, runs the engine and
-          copies the three outputs device->host; two slots let one step's
-          copies overlap its neighbours' compute, and the events span all
-          steps, copies included
+          copies the three outputs device->host (each kind of image and
+          output of a step in one page-locked arena, copied whole); two
+          slots let one step's copies overlap its neighbours' compute, and
+          the events span all steps, copies included
   roofline  the aggregation kernels of one step, each timed with CUDA events
           on its stream via the library profiler: the algorithmic bytes of
           the aggregation (4 B per voxel: the partial aggregated volume
@@ -167,21 +168,28 @@ def make_inputs(batch: int, seed0: int = 3000):
 # ---------------------------------------------------------------------------
 class MineRunner:
     def __init__(self, pairs, dev):
+        import numpy as np
         import torch
         import pyrsgm_gb300 as pg
         self.torch, self.pg = torch, pg
         self.matchers = {c: pg.StereoMatcher(W, H, pg.Params(**params_for(c))) for c in (CENSUS, BT)}
         self.costs = [c for _, _, c in pairs]
-        self.L = [torch.from_numpy(l).to(dev) for l, _, _ in pairs]
-        self.R = [torch.from_numpy(r).to(dev) for _, r, _ in pairs]
-        self.d16 = [torch.empty((H, W), dtype=torch.int16, device=dev) for _ in pairs]
-        self.d32 = [torch.empty((H, W), dtype=torch.float32, device=dev) for _ in pairs]
-        self.cf = [torch.empty((H, W), dtype=torch.float32, device=dev) for _ in pairs]
-        self.hL = [torch.from_numpy(l).pin_memory() for l, _, _ in pairs]
-        self.hR = [torch.from_numpy(r).pin_memory() for _, r, _ in pairs]
-        self.h16 = [torch.empty((H, W), dtype=torch.int16).pin_memory() for _ in pairs]
-        self.h32 = [torch.empty((H, W), dtype=torch.float32).pin_memory() for _ in pairs]
-        self.hcf = [torch.empty((H, W), dtype=torch.float32).pin_memory() for _ in pairs]
+        n = len(pairs)
+        # every image and output kind of a step in one arena (pair i at [i]),
+        # on the device and page-locked on the host: the end-to-end steps copy
+        # whole arenas, the engine gets per-pair views
+        self.A = dict(L=torch.from_numpy(np.stack([l for l, _, _ in pairs])).to(dev),
+                      R=torch.from_numpy(np.stack([r for _, r, _ in pairs])).to(dev),
+                      d16=torch.empty((n, H, W), dtype=torch.int16, device=dev),
+                      d32=torch.empty((n, H, W), dtype=torch.float32, device=dev),
+                      cf=torch.empty((n, H, W), dtype=torch.float32, device=dev),
+                      hL=torch.from_numpy(np.stack([l for l, _, _ in pairs])).pin_memory(),
+                      hR=torch.from_numpy(np.stack([r for _, r, _ in pairs])).pin_memory(),
+                      h16=torch.empty((n, H, W), dtype=torch.int16).pin_memory(),
+                      h32=torch.empty((n, H, W), dtype=torch.float32).pin_memory(),
+                      hcf=torch.empty((n, H, W), dtype=torch.float32).pin_memory())
+        for k in ("L", "R", "d16", "d32", "cf", "hL", "hR", "h16", "h32", "hcf"):
+            setattr(self, k, list(self.A[k].unbind(0)))
 
     def step(self, stream, pair_events=None):
         for i, c in enumerate(self.costs):
@@ -236,24 +244,15 @@ class BatchRunner(MineRunner):
             self.slots = []
             for k in range(2):
                 if k == 0:
-                    sl = dict(L=self.L, R=self.R, d16=self.d16, d32=self.d32, cf=self.cf, arr=self.arr)
+                    sl = dict(self.A, arr=self.arr)
                 else:
-                    sl = dict(L=[t.clone() for t in self.L], R=[t.clone() for t in self.R],
-                              d16=[torch.empty_like(t) for t in self.d16], d32=[torch.empty_like(t) for t in self.d32],
-                              cf=[torch.empty_like(t) for t in self.cf])
+                    sl = {key: (t.clone() if key in ("L", "R") else torch.empty_like(t)) if t.is_cuda
+                          else (t.clone().pin_memory() if key in ("hL", "hR") else torch.empty_like(t).pin_memory())
+                          for key, t in self.A.items()}
                     items = [dict(left=sl["L"][i], right=sl["R"][i], params=pg.Params(**params_for(c)),
                                   disp16=sl["d16"][i], disp32=sl["d32"][i], conf=sl["cf"][i])
                              for i, c in enumerate(self.costs)]
                     sl["arr"] = pg.BatchEngine.make_pairs(items)
-                    sl["hL"] = [torch.empty_like(t).pin_memory() for t in self.hL]
-                    sl["hR"] = [torch.empty_like(t).pin_memory() for t in self.hR]
-                    for a, b in zip(sl["hL"] + sl["hR"], self.hL + self.hR):
-                        a.copy_(b)
-                    sl["h16"] = [torch.empty_like(t).pin_memory() for t in self.h16]
-                    sl["h32"] = [torch.empty_like(t).pin_memory() for t in self.h32]
-                    sl["hcf"] = [torch.empty_like(t).pin_memory() for t in self.hcf]
-                if k == 0:
-                    sl.update(hL=self.hL, hR=self.hR, h16=self.h16, h32=self.h32, hcf=self.hcf)
                 sl["free"] = torch.cuda.Event()
                 sl["inp"] = torch.cuda.Event()
                 sl["done"] = torch.cuda.Event()
@@ -273,19 +272,17 @@ class BatchRunner(MineRunner):
         sl = self.slots[k % 2]
         with torch.cuda.stream(self.s_h2d):
             self.s_h2d.wait_event(sl["free"])
-            for i in range(len(self.costs)):
-                sl["L"][i].copy_(sl["hL"][i], non_blocking=True)
-                sl["R"][i].copy_(sl["hR"][i], non_blocking=True)
+            sl["L"].copy_(sl["hL"], non_blocking=True)
+            sl["R"].copy_(sl["hR"], non_blocking=True)
             sl["inp"].record(self.s_h2d)
         stream.wait_event(sl["inp"])
         self.engine.run_pairs(sl["arr"], True, stream)
         sl["done"].record(stream)
         with torch.cuda.stream(self.s_d2h):
             self.s_d2h.wait_event(sl["done"])
-            for i in range(len(self.costs)):
-                sl["h16"][i].copy_(sl["d16"][i], non_blocking=True)
-                sl["h32"][i].copy_(sl["d32"][i], non_blocking=True)
-                sl["hcf"][i].copy_(sl["cf"][i], non_blocking=True)
+            sl["h16"].copy_(sl["d16"], non_blocking=True)
+            sl["h32"].copy_(sl["d32"], non_blocking=True)
+            sl["hcf"].copy_(sl["cf"], non_blocking=True)
             sl["free"].record(self.s_d2h)
 
     def e2e_end(self, stream):
