@@ -138,13 +138,30 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
         const size_t p = (size_t)y * W + xb;
         int dv[4], dn[4];
         float cf[4];
+        int din[4];
+        float cin[4];
+        if (np == 4 && (p & 3) == 0) {   // 8- and 16-byte loads of the four pixels
+            const uint2 a = *reinterpret_cast<const uint2*>(J.disp_raw + p);
+            const float4 c = *reinterpret_cast<const float4*>(J.conf_raw + p);
+            din[0] = (int)(int16_t)(a.x & 0xffffu);
+            din[1] = (int)(int16_t)(a.x >> 16);
+            din[2] = (int)(int16_t)(a.y & 0xffffu);
+            din[3] = (int)(int16_t)(a.y >> 16);
+            cin[0] = c.x; cin[1] = c.y; cin[2] = c.z; cin[3] = c.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int jj = imin(j, np - 1);
+                din[j] = J.disp_raw[p + jj];
+                cin[j] = J.conf_raw[p + jj];
+            }
+        }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int jj = imin(j, np - 1);
-            const int d_in = J.disp_raw[p + jj];
-            const int d = (check || med) ? (int)td[ty + 1][4 * tx + 1 + jj] : d_in;
+            const int d = (check || med) ? (int)td[ty + 1][4 * tx + 1 + jj] : din[j];
             dv[j] = d;
-            cf[j] = (d != d_in) ? 0.0f : J.conf_raw[p + jj];  // the check zeroes what it rejects
+            cf[j] = (d != din[j]) ? 0.0f : cin[j];  // the check zeroes what it rejects
             dn[j] = d;
         }
         if (med) {

@@ -88,6 +88,20 @@ def test_c1_640x480_d64_single_scale_bt(words):
     assert int((mine["disp16"] > 0).sum()) > 640 * 480 // 2
 
 
+@pytest.mark.parametrize("D,cost", [(96, cases.CENSUS), (48, cases.BT)], ids=["census_d96", "bt_d48"])
+def test_640x480_single_scale_label_counts_outside_the_packed_kernels(D, cost):
+    """Label counts other than 16/32/64 take the lane-parallel path kernels
+    (k_path_tb, k_path_row with its fused WTA and LR check): the C1 pair at
+    full size, cost and aggregated volumes included."""
+    _need_ref()
+    case = cases._ss(f"c1_640x480_d{D}", 640, 480, D, cost, bs=5, uniq=10, post=cases.LRC, adaptive=True)
+    case["pair"] = _c1_pair()
+    mine = _runners.run_mine(case)
+    bad = _runners.compare(mine, _runners.run_ref(case))
+    assert not bad, bad
+    assert int((mine["disp16"] > 0).sum()) > 640 * 480 // 4
+
+
 @pytest.mark.parametrize("words", [0, 8])
 def test_c1_640x480_d64_one_pyramid_level_bt(words):
     _need_ref()
