@@ -516,7 +516,7 @@ def measure(runner, args, stream, flush, dev, world, dist, profile: bool, pair_t
 
 
 def serve_compare(pairs_pool, params_of, rate: float, n: int, seed: int = 5000, max_batch: int = 16,
-                  streams: int = 2, budget: int = 40 << 30, queue: int = 16) -> dict:
+                  streams: int = 2, budget: int = 40 << 30, queue: int = 64) -> dict:
     """n requests with Poisson arrivals at `rate` pairs/s, served (a) by the
     continuous-batching server and (b) by plain sequential compute() of one
     StereoMatcher per shape (one request at a time: H2D, compute, D2H).
