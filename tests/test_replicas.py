@@ -93,3 +93,19 @@ def test_result_line_keeps_the_contract_keys():
     ref = bench.result_line(argparse.Namespace(batch=32, steps=10, warmup=3, mode="batched", impl="reference"), 1,
                             _record(4146.6), _record(4146.6), {"hbm_gbs": 6795.1, "source": "measured"}, 320)
     assert ref["impl"] == "reference" and "roofline" not in ref
+
+
+def test_roofline_bytes_of_the_benchmark_pair():
+    """The algorithmic bytes the roofline divides by, for one 1920x1080
+    D=256 pyramid_levels=3 pair: levels 1920x1080, 960x540 and 480x270 with
+    16 labels and the coarse 240x135 with 32; 4 B per voxel for the
+    aggregation; both u8 views, the outputs and the pyramid on top."""
+    import bench
+    got = bench.alg_bytes(1920, 1080, bench.params_for(bench.CENSUS))
+    px = [1920 * 1080, 960 * 540, 480 * 270, 240 * 135]
+    vox = 16 * (px[0] + px[1] + px[2]) + 32 * px[3]
+    assert got["voxels"] == vox == 44_582_400
+    assert got["aggregation"] == 4 * vox
+    total = 4 * vox + 2 * sum(px) + 10 * px[0] + 12 * sum(px[1:]) + sum(2 * px[i - 1] + 2 * px[i] for i in (1, 2, 3))
+    assert got["total"] == total == 219_542_400
+    assert bench.alg_bytes(1920, 1080, bench.params_for(bench.BT)) == got
