@@ -210,6 +210,19 @@ const char* pyrsgm_gb300_version(void);
 /* Kernel launches issued by this library since the process started. */
 unsigned long long pyrsgm_gb300_launch_count(void);
 
+/* 1 in the checked build (libpyrsgm_gb300_checked.so, compiled with
+ * PYRSGM_CHECKED): there, chosen global-memory accesses of the kernels are
+ * range-checked on the device (a failed check records its site and skips
+ * the access), every launch is followed by a wait on its stream and an
+ * error check, and the batch engine captures no graphs.  0 in the default
+ * build. */
+int pyrsgm_gb300_checked(void);
+/* Failures the checked build has seen since load (launch errors and failed
+ * range checks; the call that met one returned an error), with the first
+ * one's description copied to `first` (may be NULL).  Always 0 in the
+ * default build. */
+int pyrsgm_gb300_check_report(char* first, size_t len);
+
 /* Opt-in speckle filter on an int16 disparity map (device pointer, pitch in
  * bytes), enqueued on `stream`: 4-neighbours belong to one region when
  * neither equals new_val and their values differ by at most max_diff (in the

@@ -9,7 +9,9 @@ import ctypes as C
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libpyrsgm_gb300.so")
+# PYRSGM_GB300_CHECKED=1 loads the checked build (pyrsgm_gb300.build.build(checked=True))
+CHECKED = os.environ.get("PYRSGM_GB300_CHECKED", "0") not in ("", "0")
+LIB_PATH = os.path.join(_HERE, "libpyrsgm_gb300_checked.so" if CHECKED else "libpyrsgm_gb300.so")
 
 _vp, _u8p, _i16p, _f32p = C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p
 _sz, _i, _f = C.c_size_t, C.c_int, C.c_float
@@ -110,6 +112,8 @@ _SIGS = {
     "pyrsgm_gb300_server_reserve": (_i, [_vp, _i, _i, C.POINTER(Params), _i, C.c_char_p, _sz]),
     "pyrsgm_gb300_version": (C.c_char_p, []),
     "pyrsgm_gb300_launch_count": (C.c_ulonglong, []),
+    "pyrsgm_gb300_checked": (_i, []),
+    "pyrsgm_gb300_check_report": (_i, [C.c_char_p, _sz]),
     "pyrsgm_gb300_set_packed_words": (_i, [_i]),
     "pyrsgm_gb300_set_autotune": (_i, [_i]),
     "pyrsgm_gb300_set_fused": (_i, [_i]),

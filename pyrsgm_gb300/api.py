@@ -230,6 +230,19 @@ def set_tbw(mode: int) -> int:
     return r
 
 
+def check_report() -> tuple[int, str]:
+    """Failures seen by the checked build since load and the first one's
+    description (pyrsgm_gb300_check_report); (0, "") in the default build."""
+    buf = C.create_string_buffer(256)
+    n = lib().pyrsgm_gb300_check_report(buf, 256)
+    return int(n), buf.value.decode()
+
+
+def is_checked() -> bool:
+    """Whether the loaded library is the checked build (PYRSGM_GB300_CHECKED=1)."""
+    return bool(lib().pyrsgm_gb300_checked())
+
+
 def fused_stalls(reset: bool = False) -> int:
     """Waits of the fused pass that ran out of time (pyrsgm_gb300_fused_stalls)."""
     return int(lib().pyrsgm_gb300_fused_stalls(1 if reset else 0))

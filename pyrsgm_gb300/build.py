@@ -18,6 +18,10 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libpyrsgm_gb300.so")
+# the checked build (range checks in the kernels, a synchronous check after
+# every launch): separate objects and library, loaded with PYRSGM_GB300_CHECKED=1
+BUILD_CHECKED = os.path.join(PKG, "_build_checked")
+LIB_CHECKED = os.path.join(PKG, "libpyrsgm_gb300_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -41,16 +45,16 @@ def _sources() -> list[str]:
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _flags() -> list[str]:
+def _flags(checked: bool = False) -> list[str]:
     return ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-Wall,-Wextra,-Wno-unused-parameter",
-                   "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
+                   "-I" + CSRC, "-I" + os.path.join(ROOT, "include")] + (["-DPYRSGM_CHECKED=1"] if checked else [])
 
 
-def _compile(src: str, hdr_mtime: float, verbose: bool) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+def _compile(src: str, hdr_mtime: float, verbose: bool, checked: bool = False) -> str:
+    obj = os.path.join(BUILD_CHECKED if checked else BUILD, os.path.basename(src)[:-3] + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), hdr_mtime):
         return obj
-    cmd = [nvcc(), "-c", src, "-o", obj] + _flags()
+    cmd = [nvcc(), "-c", src, "-o", obj] + _flags(checked)
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -61,21 +65,24 @@ def _compile(src: str, hdr_mtime: float, verbose: bool) -> str:
     return obj
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, jobs: int | None = None, checked: bool = False) -> str:
+    """The library (and the CLI); checked=True builds the checked library instead."""
+    out = LIB_CHECKED if checked else LIB
+    os.makedirs(BUILD_CHECKED if checked else BUILD, exist_ok=True)
     hdr_mtime = max(os.path.getmtime(h) for h in _headers())
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, hdr_mtime, verbose), srcs))
-    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
-        tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, hdr_mtime, verbose, checked), srcs))
+    if not (os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(o) for o in objs)):
+        tmp = out + ".tmp"
         cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
-    build_cli(hdr_mtime)
-    return LIB
+        os.replace(tmp, out)
+    if not checked:
+        build_cli(hdr_mtime)
+    return out
 
 
 CLI_SRC = os.path.join(PKG, "cli", "stereo_pair.cpp")
@@ -97,4 +104,4 @@ def build_cli(hdr_mtime: float) -> str:
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    print(build(verbose="-v" in sys.argv, checked="--checked" in sys.argv))

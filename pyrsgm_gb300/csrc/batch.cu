@@ -167,6 +167,7 @@ public:
         std::vector<PairPlan*> plans = acquire(pairs, val, n, st);
         std::vector<long long> sig = signature(pairs, val, n);
         if (st == nullptr || st == cudaStreamLegacy) use_graph = false;  // no capture on the legacy stream
+        if (kChecked) use_graph = false;   // the checked build waits after every launch
         if (use_graph) {
             for (auto it = graphs_.begin(); it != graphs_.end(); ++it) {
                 if (it->sig == sig) {

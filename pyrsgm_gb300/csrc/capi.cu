@@ -20,6 +20,7 @@
 
 #include "pyrsgm/pyrsgm_c.h"
 #include "pyrsgm/pyrsgm_gb300.h"
+#include "check.h"
 #include "sgm_launch.h"
 #include "workspace.h"
 #include "trace.h"
@@ -30,6 +31,21 @@ static std::atomic<unsigned long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+// Failures seen by the checked build (check.h): how many, and the first.
+static std::atomic<int> g_check_failures{0};
+static std::mutex g_check_mu;
+static char g_check_first[256] = {0};
+void check_record(const char* kernel, int site, cudaError_t err)
+{
+    if (g_check_failures.fetch_add(1, std::memory_order_relaxed) == 0) {
+        std::lock_guard<std::mutex> lk(g_check_mu);
+        if (site != 0)
+            std::snprintf(g_check_first, sizeof g_check_first, "%s: bounds check %d failed", kernel, site);
+        else
+            std::snprintf(g_check_first, sizeof g_check_first, "%s: %s", kernel, cudaGetErrorString(err));
+    }
+}
 
 static std::atomic<int> g_packed_words{[] {
     const char* e = std::getenv("PYRSGM_GB300_PACKED_NW");
@@ -431,6 +447,17 @@ int pyrsgm_gb300_p2_table(int* d_table, int P2, float p2Alpha, float p2Beta, flo
 const char* pyrsgm_gb300_version(void) { return "0.1.0-gb300"; }
 
 unsigned long long pyrsgm_gb300_launch_count(void) { return pg::g_launches.load(std::memory_order_relaxed); }
+
+int pyrsgm_gb300_checked(void) { return pg::kChecked ? 1 : 0; }
+
+int pyrsgm_gb300_check_report(char* first, size_t len)
+{
+    if (first && len > 0) {
+        std::lock_guard<std::mutex> lk(pg::g_check_mu);
+        std::snprintf(first, len, "%s", pg::g_check_first);
+    }
+    return pg::g_check_failures.load(std::memory_order_relaxed);
+}
 
 int pyrsgm_gb300_set_packed_words(int words)
 {

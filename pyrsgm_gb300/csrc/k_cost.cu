@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(256) k_features(const __grid_constant__ Jobs<N
         const int y = y0 + rr;
         if (y >= H) break;
         const size_t p = (size_t)y * W + xb;
+        if (!PG_IN(p, np, (size_t)W * H, 9)) continue;
         if (J.cost == COST_CENSUS) {
             // bit (dy, dx) of the 4 pixels at once: bytes 2 + dx .. 5 + dx of
             // the 12-byte row window, compared with the 4 centre bytes
@@ -359,6 +360,7 @@ __global__ void __launch_bounds__(256) k_cost_census(const __grid_constant__ Job
         return (d >= lo && d <= hi) ? (uint32_t)__popc(cl ^ __ldg(&rrow[x - off - d])) : (uint32_t)fill;
     };
     int16_t* out = J.C + p * D;
+    if (!PG_IN(p * D, D, (size_t)W * J.h * D, 10)) return;
     if ((D & 7) == 0) {
         for (int d0 = 0; d0 < D; d0 += 8) {
             uint32_t w[4];
@@ -672,6 +674,7 @@ __global__ void __launch_bounds__(256, 3) k_cost_bt_tiled(const __grid_constant_
         for (int i = 0; i < 2; ++i) {
             if (!(hasq[i] && (ncl == 1 || (c == 0) == (bq[i] <= cut)))) continue;
             const int ty = warp + 8 * i;
+            if (!PG_IN(((size_t)yq[i] * W + x) * D, D, (size_t)W * H * D, 11)) continue;
             int lo, hi;
             label_range(J, x, bq[i], lo, hi);
             int16_t* out = J.C + ((size_t)yq[i] * W + x) * D;
@@ -766,7 +769,7 @@ cudaError_t launch_pyrdown(const PyrDownBatch<NB>& b, int max_dw, int max_dh, cu
         for (int i = 0; i < b.n; ++i) by += (double)b.d[i].sw * b.d[i].sh + (double)b.d[i].dw * b.d[i].dh;
         prof_end(PK_PYRDOWN, by, st);
     }
-    return cudaGetLastError();
+    return launched(st, "k_pyrdown");
 }
 template cudaError_t launch_pyrdown<1>(const PyrDownBatch<1>&, int, int, cudaStream_t);
 template cudaError_t launch_pyrdown<2>(const PyrDownBatch<2>&, int, int, cudaStream_t);
@@ -778,7 +781,7 @@ cudaError_t launch_p2_table(int* lut, int P2, float alpha, float beta, float low
     k_p2_table<<<1, 256, 0, st>>>(lut, P2, alpha, beta, lower, upper);
     count_launch();
     prof_end(PK_P2TABLE, 1024.0, st);
-    return cudaGetLastError();
+    return launched(st, "k_p2_table");
 }
 
 template <int NJ>
@@ -799,7 +802,7 @@ cudaError_t launch_prepare(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStrea
         }
         prof_end(PK_FEATURES, by, st);
     }
-    return cudaGetLastError();
+    return launched(st, "k_features");
 }
 
 // All jobs in `jobs` share the cost mode and the refine flag.
@@ -834,7 +837,7 @@ cudaError_t launch_cost(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t
     count_launch();
     // write the int16 volume, read both views' features (and the label base)
     prof_end(PK_COST, jobs_vox(jobs) * 2 + jobs_px(jobs) * ((J0.cost == COST_CENSUS ? 8 : 32) + (J0.refine ? 2 : 0)), st);
-    return cudaGetLastError();
+    return launched(st, J0.cost == COST_CENSUS ? "k_cost_census" : J0.refine ? "k_cost_bt_tiled" : "k_cost_bt_box");
 }
 
 #define PG_INST(NJ)                                                                          \

@@ -570,7 +570,7 @@ cudaError_t launch_paths_fused16(const Jobs<NJ>& jobs, const LevelExtent& e, cud
     un.total = total;
     k_fused_reset<NJ><<<jobs.n, 32, 0, st>>>(jobs);
     count_launch();
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if ((err = launched(st, "k_fused_reset")) != cudaSuccess) return err;
     constexpr size_t smem = fz::tblr_smem<NJ>();
     if ((err = cudaFuncSetAttribute(k_tblr<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
         cudaSuccess)
@@ -596,7 +596,7 @@ cudaError_t launch_paths_fused16(const Jobs<NJ>& jobs, const LevelExtent& e, cud
         }
         prof_end(PK_TBLR, by, st);
     }
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if ((err = launched(st, "k_tblr")) != cudaSuccess) return err;
     constexpr size_t smem2 = fz::rlw_smem();
     if ((err = cudaFuncSetAttribute(k_rlw<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2)) !=
         cudaSuccess)
@@ -616,7 +616,7 @@ cudaError_t launch_paths_fused16(const Jobs<NJ>& jobs, const LevelExtent& e, cud
         }
         prof_end(PK_RLW, by, st);
     }
-    return cudaGetLastError();
+    return launched(st, "k_rlw");
 }
 
 }  // namespace pg

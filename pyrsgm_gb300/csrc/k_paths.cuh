@@ -400,7 +400,8 @@ __global__ void __launch_bounds__(kTbWarps * 32) k_path_tb(const __grid_constant
                 if (y + kPF < H) prefetch<K, PYR>(J, y + kPF, x, gl, false, ring[j]);
                 int L[K];
                 chain_step<G, K, PYR>(s, in, J.P1, J.D, gl, xb, L);
-                if (active) store_labels<K>(J.V + ((size_t)y * J.w + x) * J.D, J.D, gl, L);
+                if (active && PG_IN(((size_t)y * J.w + x) * J.D, J.D, (size_t)J.w * H * J.D, 12))
+                    store_labels<K>(J.V + ((size_t)y * J.w + x) * J.D, J.D, gl, L);
             }
         }
     }
@@ -570,7 +571,7 @@ __global__ void __launch_bounds__(32) k_path_row(const __grid_constant__ Jobs<NJ
             int16_t* b = band + (x - band_lo) * DP + gl * K;
 #pragma unroll
             for (int k = 0; k < K; ++k) b[k] = (int16_t)part[k];
-        } else if (active) {
+        } else if (active && PG_IN(((size_t)y * W + x) * D, D, (size_t)W * H * D, 13)) {
             store_labels<K>(J.V + ((size_t)y * W + x) * D, D, gl, part);
         }
     };
@@ -732,7 +733,7 @@ cudaError_t launch_paths_shape(const Jobs<NJ>& jobs, const LevelExtent& e, cudaS
         count_launch();
         // read C, write V (int16 per voxel); label base per pixel on refine levels
         prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * (tbj.d[0].refine ? 2 : 0), st);
-        if ((err = cudaGetLastError()) != cudaSuccess) return err;
+        if ((err = launched(st, "k_path_tb")) != cudaSuccess) return err;
     }
     constexpr int RPW = 32 / G;
     constexpr int DP = G * K;
@@ -756,7 +757,7 @@ cudaError_t launch_paths_shape(const Jobs<NJ>& jobs, const LevelExtent& e, cudaS
         }
         prof_end(PK_PATH_ROW, by, st);
     }
-    return cudaGetLastError();
+    return launched(st, "k_path_row");
 }
 
 // Words per thread of the packed kernels for a launch: 8 (one thread per

@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_gtb(const __grid_co
     size_t oc = oi, pc = pi, lc = li;
     int yi = 0;
     auto issue_next = [&](int slot) {
-        if (yi < H) {
+        if (yi < H && PG_IN(oi, 2 * NW, (size_t)W * H * D, 1)) {
             uint32_t* d = ring + slot * 32 * RS;
             if constexpr (NW == 8) {
                 cp16(d + ring_half(0, lane), Cg + oi);
@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_gtb(const __grid_co
         }
         if (PYR && !J.refine) mask_labels<NW>(cc, lo, hi, k);
         gstep<NW, T, PYR>(s, cc, base, p2, p12, chain + (G::NBUF == 2 ? (y & 1) * G::BUFW : 0), k);
-        if (col_ok) stw<NW>(reinterpret_cast<uint32_t*>(Vg + oc), s.L);
+        if (col_ok && PG_IN(oc, 2 * NW, (size_t)W * H * D, 2)) stw<NW>(reinterpret_cast<uint32_t*>(Vg + oc), s.L);
         oc += vstep;
         pc += W;
         lc += lstep;
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
             const size_t src = ((size_t)crow * W + (cxs + cdx * t)) * D + coff;
 #pragma unroll
             for (int j = 0; j < NCOP; ++j)
-                if (crow + 2 * j < H)
+                if (crow + 2 * j < H && PG_IN(src + j * rstride, 8, (size_t)W * H * D, 3))
                     cp16(ring + slot * SLOTW + piece_col(4 * j + (lane >> 3), pce), Cg + src + j * rstride);
         }
         // label bases and image bytes of this lane's own chain: [2 * CH][32]
@@ -699,7 +699,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow(const __grid_c
                 const size_t dst = ((size_t)crow * W + (cxs + cdx * t)) * D + coff;
 #pragma unroll
                 for (int j = 0; j < NCOP; ++j)
-                    if (crow + 2 * j < H)
+                    if (crow + 2 * j < H && PG_IN(dst + j * rstride, 8, (size_t)W * H * D, 4))
                         *reinterpret_cast<uint4*>(Og + dst + j * rstride) =
                             *reinterpret_cast<const uint4*>(ob + piece_col(4 * j + (lane >> 3), pce));
             }
@@ -774,7 +774,7 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow_lane(const __g
     size_t oc = oi, pc = pi, lc = li;
     int ti = 0;
     auto issue_next = [&](int slot) {
-        if (ti < n_mine) {
+        if (ti < n_mine && PG_IN(oi, 2 * NW, (size_t)W * J.h * D, 5)) {
             cpw<NW>(ring + slot * 32 * RS, Cg + oi);
             if (use_base) cp4(bi + slot * 64, word_of(Bg + pi));
             if (adaptive) cp4(bi + slot * 64 + 32, word_of(Lg + li));
@@ -815,7 +815,8 @@ __global__ void __launch_bounds__(pk::warps_of<NW>() * 32) k_grow_lane(const __g
             mask_labels<NW>(cc, lo, hi, k);
         }
         gstep<NW, T, PYR>(s, cc, base, p2, p12, chain + (G::NBUF == 2 ? (t & 1) * G::BUFW : 0), k);
-        if (t < n_mine && row_ok) stw<NW>(reinterpret_cast<uint32_t*>(Og + oc), s.L);
+        if (t < n_mine && row_ok && PG_IN(oc, 2 * NW, (size_t)W * J.h * D, 6))
+            stw<NW>(reinterpret_cast<uint32_t*>(Og + oc), s.L);
         oc += dxD;
         pc += dx;
         lc += dx;
@@ -979,7 +980,7 @@ __global__ void __launch_bounds__(128, 4) k_gtbw(const __grid_constant__ Jobs<NJ
     size_t pc = pi, lc = li;                     // consume cursor (row y)
     int yi = 0;
     auto issue_next = [&](int slot) {
-        if (yi < H) {
+        if (yi < H && PG_IN(oi, D, (size_t)W * H * D, 7)) {
             uint32_t* d = ring + slot * SLOT;
             cp16(d + h0, Cg + oi);
             cp16(d + h1, Cg + oi + 8);
@@ -1105,7 +1106,7 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         k_gtb<NW, T, PYR, NJ><<<g, kWarps * 32, smem, tbst>>>(tbj);
         count_launch();
         prof_end(PK_PATH_TB, jobs_vox(tbj) * 4 + jobs_px(tbj) * ((tbj.d[0].refine ? 2 : 0) + (tbj.d[0].adaptive ? 1 : 0)), tbst);
-        if ((err = cudaGetLastError()) != cudaSuccess) return err;
+        if ((err = launched(tbst, "k_gtb")) != cudaSuccess) return err;
     }
     constexpr int kWarps = pk::warps_of<NW>();
     const int rows = kWarps * G::CPW / 2;
@@ -1138,7 +1139,7 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
         }
         prof_end(PK_PATH_ROW, by, st);
     }
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if ((err = launched(st, NW == 8 ? "k_grow" : "k_grow_lane")) != cudaSuccess) return err;
     if (fork) {
         if ((err = cudaEventRecord(fk.join, fk.aux)) != cudaSuccess) return err;
         if ((err = cudaStreamWaitEvent(st, fk.join, 0)) != cudaSuccess) return err;
@@ -1155,7 +1156,7 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
             count_launch();
             prof_end(PK_TBW, jobs_vox(jobs) * 6 + jobs_px(jobs) * ((jobs.d[0].refine ? 2 : 0) + (jobs.d[0].adaptive ? 1 : 0) + 10),
                      st);
-            return cudaGetLastError();
+            return launched(st, "k_gtbw");
         }
     }
     dim3 gw((e.max_w + 31) / 32, (e.max_h + 7) / 8, jobs.n);
@@ -1163,7 +1164,7 @@ cudaError_t launch_paths_packed(const Jobs<NJ>& jobs, const LevelExtent& e, cuda
     k_wta<G::D, PYR, NJ><<<gw, 256, 0, st>>>(jobs);
     count_launch();
     prof_end(PK_WTA, jobs_vox(jobs) * 2 * (jobs.d[0].paths >= 3 ? 3 : jobs.d[0].paths) + jobs_px(jobs) * (2 + 6 + 4), st);
-    return cudaGetLastError();
+    return launched(st, "k_wta");
 }
 
 }  // namespace pg

@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256) k_post(const __grid_constant__ Jobs<NJ> j
             }
         }
         const bool vec = np == 4;
-        if (J.out16) {
+        if (J.out16 && PG_IN((size_t)y * J.out16_pitch + xb, np, (size_t)J.out16_pitch * H, 8)) {
             int16_t* o = J.out16 + (size_t)y * J.out16_pitch + xb;
             if (vec && ((reinterpret_cast<uintptr_t>(o) & 7) == 0)) {
                 *reinterpret_cast<uint2*>(o) =
@@ -259,7 +259,7 @@ cudaError_t launch_post(const Jobs<NJ>& jobs, const LevelExtent& e, cudaStream_t
         }
         prof_end(PK_POST, by, st);
     }
-    return cudaGetLastError();
+    return launched(st, "k_post");
 }
 
 template cudaError_t launch_paths<1>(const Jobs<1>&, const LevelExtent&, cudaStream_t);

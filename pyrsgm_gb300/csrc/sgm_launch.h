@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "check.h"
 #include "sgm_common.cuh"
 
 namespace pg {

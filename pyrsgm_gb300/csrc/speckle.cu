@@ -170,12 +170,21 @@ extern "C" int pyrsgm_gb300_filter_speckles(short* d_disp, size_t pitch_bytes, i
     pg::SpArgs A{d_disp, pitch_bytes / sizeof(short), width, height, new_val, max_speckle_size, max_diff,
                  static_cast<int*>(scratch), static_cast<int*>(scratch) + n};
     const dim3 g((width + 31) / 32, (height + 7) / 8);
+    cudaError_t e;
     pg::k_sp_tile<<<g, 256, 0, stream>>>(A);
-    pg::k_sp_link<<<g, 256, 0, stream>>>(A);
-    pg::k_sp_count<<<g, 256, 0, stream>>>(A);
-    pg::k_sp_apply<<<g, 256, 0, stream>>>(A);
+    if ((e = pg::launched(stream, "k_sp_tile")) == cudaSuccess) {
+        pg::k_sp_link<<<g, 256, 0, stream>>>(A);
+        e = pg::launched(stream, "k_sp_link");
+    }
+    if (e == cudaSuccess) {
+        pg::k_sp_count<<<g, 256, 0, stream>>>(A);
+        e = pg::launched(stream, "k_sp_count");
+    }
+    if (e == cudaSuccess) {
+        pg::k_sp_apply<<<g, 256, 0, stream>>>(A);
+        e = pg::launched(stream, "k_sp_apply");
+    }
     pg::count_launches(4);
-    const cudaError_t e = cudaGetLastError();
     cudaFreeAsync(scratch, stream);
     return e == cudaSuccess ? 0 : -1;
 }

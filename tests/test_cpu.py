@@ -240,6 +240,12 @@ def test_kernel_form_switches_without_device_work():
         pg.set_fused(prev_f)
 
 
+def test_default_library_is_not_the_checked_build():
+    import pyrsgm_gb300 as pg
+    assert pg.is_checked() is False
+    assert pg.check_report() == (0, "")
+
+
 def test_new_entry_points_reject_bad_arguments_without_device_work():
     """Speckle filter, plan reservation and the autotune table check their
     arguments before any device call."""
