@@ -193,9 +193,9 @@ int pyrsgm_gb300_server_inject_failure(void* server, int batches);
 int pyrsgm_gb300_server_register(void* server, void* host, size_t bytes, char* err, size_t err_len);
 /* Plans for `count` pairs of one shape kept resident in the server's pool,
  * which all stream lanes share, and device and pinned input/output buffers
- * for `count` pairs of that size on every lane (returns when allocated): a
- * server expecting bursts of one shape keeps that many resident, so no
- * request waits for an allocation. */
+ * for a full batch (max_batch pairs) of that size on every lane (returns
+ * when allocated): a server expecting bursts of one shape keeps that many
+ * resident, so no request waits for an allocation. */
 int pyrsgm_gb300_server_reserve(void* server, int width, int height, const pyrsgm_gb300_params* params, int count,
                                 char* err, size_t err_len);
 int pyrsgm_gb300_server_unregister(void* server, void* host);

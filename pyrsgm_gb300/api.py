@@ -404,7 +404,7 @@ class Server:
 
     def reserve(self, width: int, height: int, params: Params, count: int) -> None:
         """Keep plans for `count` pairs of this shape resident in the shared
-        pool, and I/O buffers for `count` pairs of this size on every lane
+        pool, and I/O buffers for a full batch of this size on every lane
         (pyrsgm_gb300_server_reserve)."""
         err = C.create_string_buffer(256)
         if lib().pyrsgm_gb300_server_reserve(self._h, width, height, C.byref(params.to_c()), count, err, 256) != 0:

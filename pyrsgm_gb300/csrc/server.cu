@@ -321,10 +321,11 @@ public:
     }
 
     // Plans for `count` pairs of one shape in the shared engine, and device
-    // and pinned I/O buffers for `count` pairs of that size on every lane,
-    // allocated now: a batch of up to `count` such pairs then allocates
-    // nothing (a cudaHostAlloc inside the stream stalls the scheduler for
-    // milliseconds).
+    // and pinned I/O buffers for a full batch (max_batch pairs) of that size
+    // on every lane, allocated now: batches of up to `count` such pairs then
+    // allocate nothing (a cudaHostAlloc inside the stream stalls the
+    // scheduler for milliseconds, and pairs of one size may fill a batch
+    // whatever their parameters).
     int reserve(int w, int h, const pyrsgm_gb300_params& prm, int count, std::string& err)
     {
         try {
@@ -334,7 +335,7 @@ public:
             std::lock_guard<std::mutex> lk(pool_mu_);
             for (auto& L : lanes_) {
                 auto& vec = L->pool[{w, h}];
-                while ((int)vec.size() < count) {
+                while ((int)vec.size() < std::max(count, max_batch_)) {
                     vec.emplace_back(new IOBuf());
                     vec.back()->alloc(w, h);
                 }
