@@ -1,7 +1,7 @@
 /* A plain C caller of the library (C99, no C++): includes every public C
  * header, links against libpyrsgm_gb300.so and exercises calls that need no
- * GPU -- argument rejection, parameter validation, level geometry, file I/O
- * and metrics.  Prints "ok" and exits 0 when every check holds. */
+ * GPU -- argument rejection, parameter validation, level geometry, the
+ * kernel-form switches, file I/O and metrics.  Prints "ok" and exits 0 when every check holds. */
 #include <stdio.h>
 #include <string.h>
 
@@ -58,6 +58,13 @@ int main(int argc, char** argv)
         CHECK(pyrsgm_gb300_read_pgm(argv[1], back, 4, &w, &h, err, sizeof err) == 0 &&
               memcmp(img, back, sizeof img) == 0);
     }
+    /* kernel-form switches and the checked-build report (host state only) */
+    int prev = pyrsgm_gb300_set_tbw(2);
+    CHECK(pyrsgm_gb300_set_tbw(prev) == 2);
+    CHECK(pyrsgm_gb300_set_tbw(3) == -1);
+    CHECK(pyrsgm_gb300_checked() == 0);
+    CHECK(pyrsgm_gb300_check_report(err, sizeof err) == 0 && err[0] == 0);
+
     float d[4] = {1.0f, 2.0f, 0.0f, 4.5f}, g[4] = {1.0f, 4.0f, 3.0f, 4.0f};
     pyrsgm_gb300_metrics m;
     CHECK(pyrsgm_gb300_evaluate(d, 4, g, 4, NULL, 0, 4, 1, 100.0f, &m) == 0);
