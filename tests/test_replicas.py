@@ -90,6 +90,14 @@ def test_result_line_keeps_the_contract_keys():
     assert out["throughput"]["mpix_per_s"] == round(out["value"] * 1920 * 1080 / 1e6, 1)
     assert set(out["kernels_hbm"]) == {"path_row", "cost"}
     assert out["kernels_ms_per_step"]["path_row"] == 2.8
+    # traffic: each aggregation kind's own bytes times its DRAM bytes per own byte
+    assert out["roofline"]["traffic"] == round(bench.AGG_TRAFFIC_PER_OWN_BYTE["path_row"] * 11.9, 4)
+    prof2 = dict(prof, tbw={"ms": 1.8, "launches": 1, "bytes": 7.0e9}, wta={"ms": 0.4, "launches": 3, "bytes": 2.0e9})
+    out2 = bench.result_line(args, 1, _record(132.7, prof2), _record(384.0), {"hbm_gbs": 6795.1, "source": "measured"},
+                             320)
+    want = sum(bench.AGG_TRAFFIC_PER_OWN_BYTE[k] * prof2[k]["bytes"] for k in ("path_row", "wta", "tbw")) / 1e9
+    assert out2["roofline"]["traffic"] == round(want, 4)
+    assert "k_gtbw" in out2["roofline"]["kernel"] and out2["roofline"]["ms_per_step"] == round(2.8 + 0.4 + 1.8, 4)
     ref = bench.result_line(argparse.Namespace(batch=32, steps=10, warmup=3, mode="batched", impl="reference"), 1,
                             _record(4146.6), _record(4146.6), {"hbm_gbs": 6795.1, "source": "measured"}, 320)
     assert ref["impl"] == "reference" and "roofline" not in ref
